@@ -1,0 +1,110 @@
+"""Generates the golden vectors in this directory from the reference itself.
+
+Every output below is computed by the reference's own functions, compiled
+from its sources by oracle/Makefile into oracle/_ref (the sources must be
+present, so this script runs in the build container only).  Inputs come
+from the seeded generators of the library's inputs module.
+
+    python tests/golden/make_golden.py
+
+Files (numpy .npz):
+  arith_P{2,4,8,16}.npz   add/mul/sub/div/sqrt/inc_d/mul_d of 256 pairs
+                          (ddf_*/qdf_*/odf_*/hdf_*, *_double_functions.cu)
+  matmul_P*.npz           matmul{dd,qd,od,hd}f on n x n (TCcuda.cu:320-372)
+  matmul_dd64.npz         the 64^3 double-double workload (seed 0)
+  split_*.npz             split4pd/split8pd/mixsplit2 (floatybits.cu:196-342)
+  squeeze_P*.npz          *_inc_d squeeze of pp partials (TCcuda.cu:876-906)
+  mat_seed.npz            srand(seed); mat(n, p) (TCcuda.cu:14)
+  bigB2.npz               bigB2 block-Toeplitz matrix (TCcuda.cu:79-95)
+  cudant.npz              TCcudant.cpp split4pd + manualconvmult/directdotconv
+"""
+import importlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+
+inputs = importlib.import_module(
+    "multiple-double-arithmetic-matrix-matrix-multiplication_gb300.inputs")
+
+
+def mixed(rng, count, P):
+    """Half signed uniform p-doubles, half reference-style positive ones,
+    with zeros, exact powers of two and a negative tail limb planted."""
+    a = inputs.uniform_pd(rng, (count // 2,), P)
+    b = inputs.reference_pd(rng, (count - count // 2,), P)
+    x = np.concatenate([a, b])
+    x[5] = 0.0
+    x[6, 0] = 1.0
+    x[6, 1:] = 0.0
+    x[7, 0] = -0.5
+    x[9, 1] = -abs(x[9, 1])
+    return x
+
+
+def main():
+    oracle.build(ref=True)
+    rng = np.random.default_rng(20240601)
+    for P in (2, 4, 8, 16):
+        a = mixed(rng, 256, P)
+        b = mixed(rng, 256, P) * 0.625
+        d = {"a": a, "b": b}
+        for op in ("add", "mul", "sub", "div", "inc_d", "mul_d"):
+            bb = b[:, 0] if op in ("inc_d", "mul_d") else b
+            d[op] = oracle.ref_vec_op(op, P, a, bb)
+        d["sqrt"] = oracle.ref_vec_op("sqrt", P, np.abs(a))
+        np.savez_compressed(os.path.join(HERE, f"arith_P{P}.npz"), **d)
+
+        n = {2: 12, 4: 10, 8: 8, 16: 4}[P]
+        A = mixed(rng, n * n, P).reshape(n, n, P)
+        B = mixed(rng, n * n, P).reshape(n, n, P)
+        np.savez_compressed(os.path.join(HERE, f"matmul_P{P}.npz"), A=A, B=B,
+                            C=oracle.ref_matmul(P, A, B, n))
+
+        for pp_mul, kind in ((4, "split4"), (8, "split8")):
+            x = mixed(rng, 64, P)
+            np.savez_compressed(os.path.join(HERE, f"{kind}_P{P}.npz"), x=x,
+                                out=oracle.ref_split(kind, P, x))
+            xr = inputs.reference_pd(rng, (64,), P)
+            np.savez_compressed(os.path.join(HERE, f"{kind}_P{P}_refstyle.npz"), x=xr,
+                                out=oracle.ref_split(kind, P, xr))
+            pp = pp_mul * P
+            parts = oracle.ref_split(kind, P, xr) * 3.0
+            np.savez_compressed(os.path.join(HERE, f"squeeze_P{P}_pp{pp}.npz"), x=parts,
+                                y=oracle.ref_squeeze(P, pp, parts))
+    x = mixed(rng, 64, 2)
+    np.savez_compressed(os.path.join(HERE, "split_mix_P2.npz"), x=x,
+                        out=oracle.ref_split("mix", 2, x))
+
+    _, A, B = inputs.workload("dd64")
+    np.savez_compressed(os.path.join(HERE, "matmul_dd64.npz"), A=A, B=B,
+                        C=oracle.ref_matmul(2, A, B, 64))
+
+    np.savez_compressed(os.path.join(HERE, "mat_seed.npz"), seed=7, n=3, P=4,
+                        out=oracle.ref_mat(7, 3, 4))
+
+    n, pp = 3, 8
+    Bq = rng.uniform(-1, 1, size=(n, n, pp))
+    np.savez_compressed(os.path.join(HERE, "bigB2.npz"), Bq=Bq, n=n, pp=pp,
+                        out=oracle.ref_bigB2(Bq, n, pp))
+
+    n, P = 8, 4
+    A = inputs.reference_pd(rng, (n, n), P)
+    B = inputs.reference_pd(rng, (n, n), P)
+    As = oracle.ref_cudant_split4(A).reshape(n, n, 4 * P)
+    Bs = oracle.ref_cudant_split4(B).reshape(n, n, 4 * P)
+    Ap = np.ascontiguousarray(np.moveaxis(As, 2, 0))
+    Bp = np.ascontiguousarray(np.moveaxis(Bs, 2, 0))
+    np.savez_compressed(os.path.join(HERE, "cudant.npz"), A=A, B=B, As=As, Bs=Bs,
+                        conv=oracle.ref_cudant_conv(0, n, 4 * P, Ap, Bp),
+                        direct=oracle.ref_cudant_conv(1, n, 4 * P, Ap, Bp))
+
+
+if __name__ == "__main__":
+    main()
