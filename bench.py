@@ -1,0 +1,376 @@
+"""Benchmark of the multi-double GEMM path on one GB300 (or N replicas).
+
+Workload (default): quad-double C = A B, m = n = k = 8192, seed 4, hi limbs
+N(0, 1), lower limbs U[-1, 1) ulp/2 (the headline configuration).  A step is
+one whole GEMM in the BF16 slice-digit form: scale exponents, digit planes,
+diagonal GEMM on the tensor cores, renormalisation.
+
+  value    effective multi-double GFLOP/s = 2 m n k / t, inputs resident in
+           HBM, timed with CUDA events on the launching stream
+  e2e      the same metric through mdg_gemm_host-style use of the C ABI
+           with pinned host buffers: A and B copied in and C copied out
+           inside the timed region of every step
+  roofline the diagonal GEMM kernel: BF16 tensor FLOPs it must execute
+           (2 Mp Np Kp per digit pair) over its own event-timed duration
+  cpu_baseline  the oracle's plain quad-double GEMM (the C restatement of
+           the reference's matmulqdf) on the host cores, a bounded sample
+  forms    the FP64-split and plain forms on the 1024^3 quad-double
+           workload (seed 1), and error bits of every form against the
+           exact product on a sampled block
+
+--impl reference times the reference's CPU implementation of the path
+(oracle/_ref when it was built from the reference sources on this machine,
+else the oracle's restatement of it) on the same metric.
+"""
+import argparse
+import ctypes
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "multiple-double-arithmetic-matrix-matrix-multiplication_gb300"
+METRIC = "qd/od GEMM effective GFLOP/s: slice-TC vs FP64-split vs plain, equal error bits"
+UNIT = "GFLOP/s"
+
+WORKLOADS = {
+    "qd8192_normal": "qd8192_normal",
+    "qd1024": "qd1024",
+    "od2048_spread": "od2048_spread",
+    "dd64": "dd64",
+}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return d["bf16_tflops"], d["bf16_tflops_sustained"], d["hbm_gbs"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, 1700.0, 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", os.environ.get("LOCAL_RANK", "0"),
+                 f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return world, rank
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(P, A, B, target_s, threads):
+    """Time the oracle's plain GEMM (the reference's matmulqdf arithmetic) on
+    R rows x nc columns of C at the full k, sized to take about target_s."""
+    import oracle
+    k = A.shape[1]
+    r, nc = 1, 8
+    Bs = np.ascontiguousarray(B[:, :nc])
+    t0 = time.perf_counter()
+    oracle.gemm_plain(P, A[:r], Bs, r, nc, k, threads=1)
+    per_madd = (time.perf_counter() - t0) / (r * nc * k)
+    madds = max(1.0, target_s / per_madd) * threads
+    nc = int(min(B.shape[1], max(threads, 64)))
+    r = int(max(threads, min(A.shape[0], madds / (nc * k))))
+    r = (r // threads) * threads or threads
+    Bs = np.ascontiguousarray(B[:, :nc])
+    t0 = time.perf_counter()
+    oracle.gemm_plain(P, A[:r], Bs, r, nc, k, threads=threads)
+    dt = time.perf_counter() - t0
+    return 2.0 * r * nc * k / dt / 1e9, f"{r} rows x {nc} columns of C at k={k}", dt
+
+
+def run_reference(args):
+    """The reference's CPU path, timed on the host cores."""
+    world, rank = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    inputs = importlib.import_module(PKG + ".inputs")
+    oracle.build()
+    threads = os.cpu_count() or 1
+    P, A, B = inputs.workload(args.workload)
+    kind = "port"
+    if oracle.ref_available():
+        kind = "reference"
+    vals = []
+    for i in range(args.warmup + args.steps):
+        if kind == "reference":
+            # square sub-problem through the reference's matmulqdf, one per thread
+            import concurrent.futures as cf
+            nsub = 96
+            Asub = np.ascontiguousarray(A[:nsub, :nsub])
+            Bsub = np.ascontiguousarray(B[:nsub, :nsub])
+            t0 = time.perf_counter()
+            with cf.ThreadPoolExecutor(threads) as ex:
+                list(ex.map(lambda _: oracle.ref_matmul(P, Asub, Bsub, nsub), range(threads)))
+            dt = time.perf_counter() - t0
+            v = 2.0 * nsub ** 3 * threads / dt / 1e9
+            sample = f"{threads} x matmulqdf n={nsub} (reference sources)"
+        else:
+            v, sample, dt = cpu_sample(P, A, B, 3.0, threads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def event_time(fn, stream, iters=1):
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(iters):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / iters
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="qd8192_normal", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-forms", action="store_true", help="skip the FP64-split/plain lines")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    world, rank = dist_setup(args.gpus)
+    api = importlib.import_module(PKG + ".api")
+    _lib = importlib.import_module(PKG + "._lib")
+    inputs = importlib.import_module(PKG + ".inputs")
+    L = _lib.lib()
+    stream = torch.cuda.current_stream()
+
+    P, A, B = inputs.workload(args.workload)
+    m, k = A.shape[:2]
+    n = B.shape[1]
+    flops = 2.0 * m * n * k
+    s = api.default_slices(P)
+    D = s
+    dA = torch.from_numpy(A).cuda()
+    dB = torch.from_numpy(B).cuda()
+    dC = torch.empty((m, n, P), dtype=torch.float64, device="cuda")
+    need = api.workspace_size("slice_bf16", P, m, n, k)
+    ws = torch.empty(need, dtype=torch.uint8, device="cuda")
+
+    def step():
+        api.gemm(dA, dB, "slice_bf16", out=dC, workspace=ws)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timing (inputs larger than L2)
+    clocks = Clocks()
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    t_step = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, world)
+    clk = clocks.stop()
+    value = flops * world / t_step / 1e9
+
+    # ---- roofline of the diagonal GEMM: run the stages once, time it alone
+    pl_Mp, pl_Np, pl_Kp = [-(-x // a) * a for x, a in ((m, 128), (n, 128), (k, 64))]
+    E, F = api.scale_exponents(dA, dB)
+    pa = api.slice_digits(dA, E, s)
+    pb = api.slice_digits(dB, F, s, trans=True)
+    pa_p = torch.zeros((s, pl_Mp, pl_Kp), dtype=torch.bfloat16, device="cuda")
+    pb_p = torch.zeros((s, pl_Np, pl_Kp), dtype=torch.bfloat16, device="cuda")
+    pa_p[:, :m, :k] = pa
+    pb_p[:, :n, :k] = pb
+    del pa, pb
+    api.slice_diagonals(pa_p, pb_p, D)
+    t_diag = event_time(lambda: api.slice_diagonals(pa_p, pb_p, D), stream, iters=2)
+    pairs = sum(min(d, s - 1) - max(0, d - (s - 1)) + 1 for d in range(D))
+    tflop = 2.0 * pl_Mp * pl_Np * pl_Kp * pairs / 1e12
+    bf16_burst, bf16_sust, hbm, peak_kind = peaks()
+    achieved = tflop / t_diag
+    del pa_p, pb_p
+    torch.cuda.empty_cache()
+
+    # ---- e2e through the C ABI with pinned host buffers
+    hA = torch.from_numpy(A).pin_memory()
+    hB = torch.from_numpy(B).pin_memory()
+    hC = torch.empty((m, n, P), dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        dA.copy_(hA, non_blocking=True)
+        dB.copy_(hB, non_blocking=True)
+        api.gemm(dA, dB, "slice_bf16", out=dC, workspace=ws)
+        hC.copy_(dC, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world)
+    assert np.array_equal(hC.numpy(), dC.cpu().numpy())
+
+    # ---- error bits on a sampled block against the exact product
+    import oracle.exact as ex
+    rows, cols = range(0, m, max(1, m // 6)), range(0, n, max(1, n // 6))
+    C_tc = dC.cpu().numpy()
+    bits = {"slice_bf16": ex.error_bits(C_tc, A, B, rows, cols)}
+
+    forms = None
+    if not args.no_forms and rank == 0:
+        forms = {}
+        P2, A2, B2 = inputs.workload("qd1024")
+        dA2, dB2 = torch.from_numpy(A2).cuda(), torch.from_numpy(B2).cuda()
+        r2, c2 = range(0, 1024, 200), range(0, 1024, 200)
+        for form in ("slice_bf16", "fp64split", "plain"):
+            out = torch.empty((1024, 1024, P2), dtype=torch.float64, device="cuda")
+            w2 = torch.empty(max(1, api.workspace_size(form, P2, 1024, 1024, 1024)),
+                             dtype=torch.uint8, device="cuda")
+            api.gemm(dA2, dB2, form, out=out, workspace=w2)
+            t = event_time(lambda: api.gemm(dA2, dB2, form, out=out, workspace=w2), stream,
+                           iters=2 if form == "slice_bf16" else 1)
+            eb = ex.error_bits(out.cpu().numpy(), A2, B2, r2, c2)
+            forms[form] = {"workload": "qd1024", "gflops": 2.0 * 1024 ** 3 / t / 1e9,
+                           "ms": t * 1e3, "error_bits_entrywise": round(eb[0], 1),
+                           "error_bits_normwise": round(eb[1], 1)}
+        if "fp64split" in forms:
+            forms["slice_over_fp64split"] = forms["slice_bf16"]["gflops"] / forms["fp64split"]["gflops"]
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        v, sample, _ = cpu_sample(P, A, B, 6.0, os.cpu_count() or 1)
+        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+            "data": "synthetic (seeded numpy generators, shapes/distributions of the workload)",
+            "config": {"workload": args.workload, "p": P, "m": m, "n": n, "k": k, "slices": s,
+                       "diagonals": D, "digit_pairs": pairs, "form": "slice_bf16",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "inputs (2 x 2 GiB) larger than L2, no flush"},
+            "e2e": {"value": flops * world / t_e2e / 1e9, "unit": UNIT,
+                    "h2d_bytes_per_step": A.nbytes + B.nbytes,
+                    "d2h_bytes_per_step": m * n * P * 8},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_sust,
+                         "unit": "TFLOP/s", "frac": achieved / bf16_sust, "traffic": None,
+                         "kernel": "diag_gemm", "kernel_ms": t_diag * 1e3,
+                         "algorithmic_tflop_per_launch": tflop,
+                         "peak_kind": f"{peak_kind} bf16 sustained"},
+            "gpu_launches": 8 * args.steps,
+            "clocks": clk,
+            "error_bits": {"slice_bf16": [round(x, 1) for x in bits["slice_bf16"]],
+                           "sample": f"{len(rows)}x{len(cols)} entries, exact integer product"},
+            "cpu_baseline": cpu,
+            "forms": forms,
+        }
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,175 @@
+/*
+ * mdgemm.h -- C ABI of the GB300 multi-double GEMM library (libmdgemm.so).
+ *
+ * Plain C types only: device pointers, sizes, a cudaStream_t passed as
+ * void*.  Every entry point returns an mdg_status; none of them exits or
+ * throws.  Matrices of P-doubles are row-major with the P limbs of one
+ * entry contiguous, most significant first, the layout of the reference
+ * (C++/TCcuda.cu:130-131): entry (r, c) limb l of a matrix with leading
+ * dimension ld (in entries) is at  ptr[(r * ld + c) * P + l].
+ *
+ * Each function names the reference interface it replaces.  The reference
+ * surface is C++ (C++/TCcuda.h:23-103, C++/floatybits.h:17-97); its
+ * std::vector wrappers are provided on top of this ABI by TCcuda.h and
+ * floatybits.h in this directory.
+ */
+#ifndef MDGEMM_H
+#define MDGEMM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  MDG_SUCCESS = 0,
+  MDG_ERROR_INVALID_LIMBS = 1,  /* P not in {2, 4, 8, 16} (or not allowed for this call) */
+  MDG_ERROR_INVALID_SIZE = 2,   /* negative size, leading dimension too small, size too large */
+  MDG_ERROR_NULL_POINTER = 3,   /* a required pointer is NULL */
+  MDG_ERROR_INVALID_FORM = 4,   /* unknown form or option value */
+  MDG_ERROR_WORKSPACE = 5,      /* workspace missing or smaller than *_workspace_size */
+  MDG_ERROR_CUDA = 6,           /* a CUDA call failed, see mdg_last_cuda_error() */
+  MDG_ERROR_NOT_SUPPORTED = 7,  /* valid request this build cannot serve */
+  MDG_ERROR_TIMEOUT = 8,        /* a bounded device-side wait gave up */
+  MDG_ERROR_ALLOCATION = 9      /* device or pinned allocation failed */
+} mdg_status;
+
+/* GEMM forms. */
+enum {
+  /* The plain multi-double GEMM on FP64 CUDA cores: one product and one
+   * addition per step with the reference's arithmetic, bit for bit the
+   * result of matmul{dd,qd,od,hd}f (TCcuda.cu:320-372) and of matmulTCnt
+   * compiled without contraction (TCcuda.cu:248-302). */
+  MDG_FORM_PLAIN = 0,
+  /* The reference's own split method: every limb cut into 13-bit (or
+   * 7-bit) FP64 slices (floatybits.cu:196,303,327), the truncated slice
+   * convolution on FP64 DMMA tensor cores (TCtest.cu:21-46 against the
+   * block-Toeplitz bigB2, TCcuda.cu:79-95), then the squeeze of the
+   * partial sums (TCcuda.cu:876-958). */
+  MDG_FORM_FP64_SPLIT = 1,
+  /* Slice digits on BF16 tensor cores: exact 8-bit balanced digits per
+   * operand with a shared exponent per row of A / column of B, exact
+   * diagonal sums (FP32 accumulation flushed every 256 products into
+   * integers), exact rounding back to P limbs.  No reference counterpart:
+   * this is the tensor-core form the reference set out to build. */
+  MDG_FORM_SLICE_BF16 = 2
+};
+
+/* Options; a NULL pointer or zero fields mean the defaults. */
+typedef struct {
+  int slices;       /* BF16 form: digits per operand (0: default for P) */
+  int diagonals;    /* BF16 form: diagonals kept, 1..2*slices-1 (0: = slices) */
+  int split_kind;   /* FP64 form: 0 split4 (pp=4P), 1 split8 (pp=8P), 2 mixed dd (pp=12) */
+  int split_exact;  /* FP64 form: 0 or 1 = exact slices (default), 2 = reference-compatible */
+  int reserved[4];
+} mdg_options;
+
+/* One problem of a batched call. */
+typedef struct {
+  int p, m, n, k;
+  const double *A;  /* device, m x k, leading dimension lda */
+  const double *B;  /* device, k x n */
+  double *C;        /* device, m x n */
+  int lda, ldb, ldc;
+} mdg_problem;
+
+const char *mdg_status_string(int status);
+/* Text of the last CUDA error seen by the calling thread ("" if none). */
+const char *mdg_last_cuda_error(void);
+int mdg_version(void);
+
+/* Default number of BF16 digits for P limbs. */
+int mdg_default_slices(int p);
+
+/* ---------------------------------------------------------------- GEMM -- */
+
+/* Bytes of device workspace mdg_gemm needs for this problem (0 for the
+ * plain form).  Replaces the cudaMalloc calls inside matmulTCnt and
+ * TCtest.cu:73-82, which the reference never frees. */
+size_t mdg_gemm_workspace_size(int form, int p, int m, int n, int k,
+                               const mdg_options *opt);
+
+/* C = A * B, all device pointers, asynchronous on `stream`.
+ * Replaces matmulTCnt (TCcuda.cu:248, form PLAIN) and the split GEMM of
+ * TCtest.cu:48-114 (form FP64_SPLIT); any m, n, k >= 0. */
+int mdg_gemm(int form, int p, int m, int n, int k, const double *A, int lda,
+             const double *B, int ldb, double *C, int ldc,
+             const mdg_options *opt, void *workspace, size_t workspace_bytes,
+             void *stream);
+
+/* C = A * B with HOST buffers: copies in, computes, copies out, waits.
+ * Device memory comes from a cache owned by the library (freed by
+ * mdg_release_cache).  This is the call the std::vector wrappers make. */
+int mdg_gemm_host(int form, int p, int m, int n, int k, const double *A,
+                  const double *B, double *C, const mdg_options *opt);
+
+/* Many independent problems with mixed P and sizes in one persistent
+ * launch per stage (plain: one launch in all).  No reference counterpart
+ * (the reference runs one square problem per call). */
+size_t mdg_gemm_batched_workspace_size(int form, const mdg_problem *problems,
+                                       int count, const mdg_options *opt);
+int mdg_gemm_batched(int form, const mdg_problem *problems, int count,
+                     const mdg_options *opt, void *workspace,
+                     size_t workspace_bytes, void *stream);
+
+void mdg_release_cache(void);
+
+/* ------------------------------------------------- FP64 split stages -- */
+
+/* Slices of `count` P-doubles: kind 0 split4pd (floatybits.cu:196),
+ * 1 split8pd (:303), 2 mixsplit2 (:327, P must be 2).  exact = 0 gives the
+ * reference's slices bit for bit, quirks included (a negative limb gives
+ * zero slices, the 53rd significand bit is dropped); exact = 1 keeps sign
+ * and all bits.  out: count x pp doubles (pp = 4P, 8P or 12). */
+int mdg_split(int kind, int exact, int p, long long count, const double *x,
+              double *out, void *stream);
+
+/* y_i = sum_j x[i*pp + j] through the P-double inc_d, j in order; y is
+ * count x P.  Replaces pllsqueeze_old (TCcuda.cu:908) and its kernels
+ * pllsqueeze_{2,4,8,16}_pp_old (TCcuda.cu:876-906); pp >= 1. */
+int mdg_squeeze(int p, int pp, long long count, const double *x, double *y,
+                void *stream);
+
+/* Truncated slice convolution on FP64 tensor cores:
+ * Cq[r][c][i] = sum_k sum_{j<=i} Aq[r][k][j] * Bq[k][c][i-j], Aq m x k x pp,
+ * Bq k x n x pp, Cq m x n x pp (the reference's matmul kernel against
+ * bigB2, TCtest.cu:21-46, TCcuda.cu:79-95, without forming bigB2). */
+size_t mdg_slice_conv_workspace_size(int pp, int m, int n, int k);
+int mdg_slice_conv(int pp, int m, int n, int k, const double *Aq,
+                   const double *Bq, double *Cq, void *workspace,
+                   size_t workspace_bytes, void *stream);
+
+/* ----------------------------------------------- BF16 slice stages -- */
+
+/* Scale exponents: E[r] for the rows of A (m x k), F[c] for the columns
+ * of B (k x n); 2^E bounds every entry of the row. */
+int mdg_scale_exponents(int p, int m, int n, int k, const double *A, int lda,
+                        const double *B, int ldb, int *E, int *F,
+                        void *stream);
+
+/* Balanced base-256 digits of a P-double matrix as BF16 planes.
+ * trans = 0: X is rows x cols (A), plane i is rows x ld_out row-major.
+ * trans = 1: X is cols x rows (B, k x n), plane i is rows(n) x ld_out,
+ * i.e. transposed so that both operands are K-major.  Planes are
+ * plane_stride elements apart.  Values are the integers d in [-128, 128]. */
+int mdg_slice_digits(int p, int s, int rows, int cols, const double *X,
+                     int ldx, const int *E, int trans, void *planes,
+                     int ld_out, long long plane_stride, void *stream);
+
+/* Exact diagonal sums Cd[d][r][c] = sum_{i+j=d} sum_k dA_i[r][k] dB_j[c][k]
+ * (int64) for d < D, on BF16 tensor cores. */
+int mdg_slice_diagonals(int s, int D, int m, int n, int k, const void *dA,
+                        const void *dB, int ld, long long plane_a,
+                        long long plane_b, long long *Cd, void *stream);
+
+/* C[r][c] = RN_P( sum_d Cd[d][r][c] 256^(D-1-d) ) * 2^(E[r]+F[c]-14-8(D-1)). */
+int mdg_renorm_diagonals(int p, int D, int m, int n, const long long *Cd,
+                         const int *E, const int *F, double *C, int ldc,
+                         void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MDGEMM_H */

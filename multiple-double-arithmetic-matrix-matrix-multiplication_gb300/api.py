@@ -1,0 +1,209 @@
+"""Python mirror of the reference's GEMM interface over the C ABI.
+
+Device arrays are torch CUDA tensors of float64 shaped (rows, cols, P),
+row-major with the limbs last (the reference layout, TCcuda.cu:130-131);
+host arrays are numpy float64 of the same shape.  Names that exist in the
+reference keep its name and argument order (matmulTCnt, split4pd,
+split8pd, mixsplit2, pllsqueeze_old, TCcuda.h:66-103, floatybits.h:76-97);
+``gemm`` is the device-resident entry of all three forms.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from ._lib import Options, Problem, check, lib
+
+FORMS = {"plain": 0, "fp64split": 1, "slice_bf16": 2}
+SPLIT_KINDS = {"split4": 0, "split8": 1, "mix": 2}
+
+
+def _opts(slices=0, diagonals=0, split_kind="split4", split_exact=True):
+    o = Options()
+    o.slices, o.diagonals = int(slices), int(diagonals)
+    o.split_kind = SPLIT_KINDS[split_kind] if isinstance(split_kind, str) else int(split_kind)
+    o.split_exact = 1 if split_exact else 2
+    return o
+
+
+def _stream(stream):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None and t.numel() else None
+
+
+def _dev(x, device="cuda"):
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=torch.float64).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).to(device)
+
+
+def default_slices(p):
+    return lib().mdg_default_slices(p)
+
+
+def workspace_size(form, p, m, n, k, **kw):
+    return lib().mdg_gemm_workspace_size(FORMS[form], p, m, n, k, ctypes.byref(_opts(**kw)))
+
+
+def gemm(A, B, form="slice_bf16", out=None, workspace=None, stream=None, **kw):
+    """C = A @ B for device tensors A (m, k, P) and B (k, n, P)."""
+    assert A.is_cuda and B.is_cuda and A.dtype == torch.float64 and B.dtype == torch.float64
+    m, k, p = A.shape
+    k2, n, p2 = B.shape
+    assert k == k2 and p == p2
+    A, B = A.contiguous(), B.contiguous()
+    C = out if out is not None else torch.empty((m, n, p), dtype=torch.float64, device=A.device)
+    opt = _opts(**kw)
+    need = lib().mdg_gemm_workspace_size(FORMS[form], p, m, n, k, ctypes.byref(opt))
+    if need and (workspace is None or workspace.numel() < need):
+        workspace = torch.empty(need, dtype=torch.uint8, device=A.device)
+    check(lib().mdg_gemm(FORMS[form], p, m, n, k, _ptr(A), max(k, 1), _ptr(B), max(n, 1),
+                         _ptr(C), max(n, 1), ctypes.byref(opt), _ptr(workspace) if need else None,
+                         need, _stream(stream)), "mdg_gemm")
+    return C
+
+
+def gemm_host(A, B, form="slice_bf16", **kw):
+    """C = A @ B for host numpy arrays through mdg_gemm_host (copies in and
+    out inside the call)."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    m, k, p = A.shape
+    n = B.shape[1]
+    C = np.empty((m, n, p), dtype=np.float64)
+    check(lib().mdg_gemm_host(FORMS[form], p, m, n, k, A.ctypes.data, B.ctypes.data,
+                              C.ctypes.data, ctypes.byref(_opts(**kw))), "mdg_gemm_host")
+    return C
+
+
+def gemm_batched(problems, form="plain", stream=None, **kw):
+    """problems: list of (A, B) device tensor pairs; returns the list of C."""
+    Cs, table, keep = [], (Problem * len(problems))(), []
+    for i, (A, B) in enumerate(problems):
+        m, k, p = A.shape
+        n = B.shape[1]
+        A, B = A.contiguous(), B.contiguous()
+        C = torch.empty((m, n, p), dtype=torch.float64, device=A.device)
+        keep += [A, B]
+        Cs.append(C)
+        table[i] = Problem(p, m, n, k, A.data_ptr(), B.data_ptr(), C.data_ptr(), max(k, 1),
+                           max(n, 1), max(n, 1))
+    opt = _opts(**kw)
+    need = lib().mdg_gemm_batched_workspace_size(FORMS[form], table, len(problems),
+                                                 ctypes.byref(opt))
+    ws = torch.empty(max(need, 1), dtype=torch.uint8, device="cuda")
+    check(lib().mdg_gemm_batched(FORMS[form], table, len(problems), ctypes.byref(opt),
+                                 _ptr(ws), need, _stream(stream)), "mdg_gemm_batched")
+    return Cs
+
+
+# --------------------------------------------------- reference-named API --
+
+def matmulTCnt(A, B, n, nfrag, p, loop_ct=1):
+    """The plain multi-double GEMM of n x n host matrices (TCcuda.cu:248):
+    returns (C, t_CUDA in ms for loop_ct launches).  nfrag is accepted for
+    compatibility; the tiling is the library's."""
+    del nfrag
+    dA = _dev(np.asarray(A).reshape(n, n, p))
+    dB = _dev(np.asarray(B).reshape(n, n, p))
+    C = torch.zeros((n, n, p), dtype=torch.float64, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(loop_ct):
+        gemm(dA, dB, "plain", out=C)
+    e1.record()
+    torch.cuda.synchronize()
+    return C.cpu().numpy().reshape(-1), e0.elapsed_time(e1)
+
+
+def _split(kind, x, p, exact=False):
+    x = _dev(np.asarray(x, dtype=np.float64).reshape(-1, p)) if not isinstance(x, torch.Tensor) else x.contiguous()
+    count = x.numel() // p
+    pp = {0: 4 * p, 1: 8 * p, 2: 12}[kind]
+    out = torch.empty((count, pp), dtype=torch.float64, device=x.device)
+    check(lib().mdg_split(kind, int(exact), p, count, _ptr(x), _ptr(out), _stream(None)),
+          "mdg_split")
+    return out
+
+
+def split4pd(x, p, exact=False):
+    """Slices of a vector of p-doubles (floatybits.cu:196); reference bits by
+    default, exact=True keeps signs and the 53rd bit."""
+    return _split(0, x, p, exact)
+
+
+def split8pd(x, p, exact=False):
+    return _split(1, x, p, exact)
+
+
+def mixsplit2(x, exact=False):
+    return _split(2, x, 2, exact)
+
+
+def pllsqueeze_old(x, p, pp):
+    """Squeeze of pp partial sums per entry into p-doubles (TCcuda.cu:908)."""
+    x = _dev(np.asarray(x, dtype=np.float64).reshape(-1)) if not isinstance(x, torch.Tensor) else x.contiguous()
+    count = x.numel() // pp
+    y = torch.empty((count, p), dtype=torch.float64, device=x.device)
+    check(lib().mdg_squeeze(p, pp, count, _ptr(x), _ptr(y), _stream(None)), "mdg_squeeze")
+    return y
+
+
+def slice_conv(Aq, Bq):
+    """Truncated slice convolution on FP64 tensor cores; Aq (m, k, pp),
+    Bq (k, n, pp) device tensors."""
+    m, k, pp = Aq.shape
+    n = Bq.shape[1]
+    Cq = torch.empty((m, n, pp), dtype=torch.float64, device=Aq.device)
+    check(lib().mdg_slice_conv(pp, m, n, k, _ptr(Aq.contiguous()), _ptr(Bq.contiguous()),
+                               _ptr(Cq), None, 0, _stream(None)), "mdg_slice_conv")
+    return Cq
+
+
+# ----------------------------------------------- slice-digit stages --
+
+def scale_exponents(A, B):
+    m, k, p = A.shape
+    n = B.shape[1]
+    E = torch.empty(max(m, 1), dtype=torch.int32, device=A.device)
+    F = torch.empty(max(n, 1), dtype=torch.int32, device=A.device)
+    check(lib().mdg_scale_exponents(p, m, n, k, _ptr(A), max(k, 1), _ptr(B), max(n, 1), _ptr(E),
+                                    _ptr(F), _stream(None)), "mdg_scale_exponents")
+    return E[:m], F[:n]
+
+
+def slice_digits(X, E, s, trans=False):
+    """BF16 digit planes: X (rows, cols, P) -> (s, rows, cols); trans=True
+    takes X as (cols, rows, P) (B) and returns planes (s, n, k)."""
+    if trans:
+        cols, rows, p = X.shape
+    else:
+        rows, cols, p = X.shape
+    planes = torch.empty((s, rows, cols), dtype=torch.bfloat16, device=X.device)
+    check(lib().mdg_slice_digits(p, s, rows, cols, _ptr(X), X.shape[1], _ptr(E), int(trans),
+                                 _ptr(planes), cols, rows * cols, _stream(None)),
+          "mdg_slice_digits")
+    return planes
+
+
+def slice_diagonals(dA, dB, D):
+    """Exact diagonal sums of digit planes dA (s, m, k), dB (s, n, k); m, n
+    multiples of 128, k of 64."""
+    s, m, k = dA.shape
+    n = dB.shape[1]
+    Cd = torch.empty((D, m, n), dtype=torch.int64, device=dA.device)
+    check(lib().mdg_slice_diagonals(s, D, m, n, k, _ptr(dA), _ptr(dB), k, m * k, n * k, _ptr(Cd),
+                                    _stream(None)), "mdg_slice_diagonals")
+    return Cd
+
+
+def renorm_diagonals(Cd, E, F, p):
+    D, m, n = Cd.shape
+    C = torch.empty((m, n, p), dtype=torch.float64, device=Cd.device)
+    check(lib().mdg_renorm_diagonals(p, D, m, n, _ptr(Cd), _ptr(E), _ptr(F), _ptr(C), n,
+                                     _stream(None)), "mdg_renorm_diagonals")
+    return C

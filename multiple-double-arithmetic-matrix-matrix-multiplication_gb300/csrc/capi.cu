@@ -1,0 +1,409 @@
+// The C ABI (include/mdgemm.h): argument checks, workspace layout, form
+// dispatch, the host-buffer entry and the batched entry.
+#include <algorithm>
+#include <cstdlib>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "slice_tc.cuh"
+
+namespace mdgi {
+
+static thread_local char g_cuda_error[256] = "";
+
+void set_cuda_error(cudaError_t e) {
+  std::snprintf(g_cuda_error, sizeof g_cuda_error, "%s: %s", cudaGetErrorName(e),
+                cudaGetErrorString(e));
+}
+
+int default_engine() {
+  const char *v = std::getenv("MDG_SLICE_ENGINE");
+  if (v && *v) return std::atoi(v) ? 1 : 0;
+  return 1;
+}
+
+// ------------------------------------------------------------------ cache --
+// Grow-only device buffers owned by the library, for calls that take no
+// workspace argument (mdg_gemm_host, mdg_scale_exponents).  One per slot.
+struct DeviceCache {
+  std::mutex mu;
+  void *ptr[4] = {nullptr, nullptr, nullptr, nullptr};
+  size_t cap[4] = {0, 0, 0, 0};
+  int get(int slot, size_t bytes, void **out) {
+    if (bytes == 0) bytes = 256;
+    if (cap[slot] < bytes) {
+      if (ptr[slot]) cudaFree(ptr[slot]);
+      ptr[slot] = nullptr;
+      cap[slot] = 0;
+      cudaError_t e = cudaMalloc(&ptr[slot], bytes);
+      if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return MDG_ERROR_ALLOCATION;
+      }
+      cap[slot] = bytes;
+    }
+    *out = ptr[slot];
+    return MDG_SUCCESS;
+  }
+  void release() {
+    std::lock_guard<std::mutex> lk(mu);
+    for (int i = 0; i < 4; ++i) {
+      if (ptr[i]) cudaFree(ptr[i]);
+      ptr[i] = nullptr;
+      cap[i] = 0;
+    }
+  }
+};
+static DeviceCache g_cache;
+
+// ---------------------------------------------------------------- checks --
+static int check_gemm_args(int form, int p, int m, int n, int k, const void *A, int lda,
+                           const void *B, int ldb, const void *C, int ldc) {
+  if (form < MDG_FORM_PLAIN || form > MDG_FORM_SLICE_BF16) return MDG_ERROR_INVALID_FORM;
+  if (!valid_p(p)) return MDG_ERROR_INVALID_LIMBS;
+  if (m < 0 || n < 0 || k < 0) return MDG_ERROR_INVALID_SIZE;
+  if (lda < std::max(k, 1) || ldb < std::max(n, 1) || ldc < std::max(n, 1))
+    return MDG_ERROR_INVALID_SIZE;
+  if (m == 0 || n == 0) return MDG_SUCCESS;  // nothing is read or written
+  if (!C || (k > 0 && (!A || !B))) return MDG_ERROR_NULL_POINTER;
+  return MDG_SUCCESS;
+}
+
+struct Opts {
+  int slices, diagonals, split_kind, split_exact;
+};
+
+static int resolve_opts(int p, const mdg_options *o, Opts *r) {
+  r->slices = (o && o->slices) ? o->slices : mdg_default_slices(p);
+  r->diagonals = (o && o->diagonals) ? o->diagonals : r->slices;
+  r->split_kind = o ? o->split_kind : 0;
+  if (o && (o->split_exact < 0 || o->split_exact > 2)) return MDG_ERROR_INVALID_FORM;
+  r->split_exact = (o && o->split_exact == 2) ? 0 : 1;
+  if (r->slices < 1 || r->slices > 128) return MDG_ERROR_INVALID_FORM;
+  if (r->diagonals < 1 || r->diagonals > 2 * r->slices - 1) return MDG_ERROR_INVALID_FORM;
+  if (r->split_kind < 0 || r->split_kind > 2) return MDG_ERROR_INVALID_FORM;
+  if (r->split_kind == 2 && p != 2) return MDG_ERROR_INVALID_LIMBS;
+  if (!words_for(r->slices, r->diagonals)) return MDG_ERROR_NOT_SUPPORTED;
+  return MDG_SUCCESS;
+}
+
+static int split_pp(int kind, int p) { return kind == 0 ? 4 * p : kind == 1 ? 8 * p : 12; }
+
+// FP64 split form workspace: packed A/B (when strided), slices, partials,
+// packed C (when strided).
+struct SplitPlan {
+  int pp;
+  size_t off_Ap, off_Bp, off_Aq, off_Bq, off_Cq, off_Cp, total;
+};
+
+static SplitPlan make_split_plan(int p, int kind, int m, int n, int k) {
+  SplitPlan s{};
+  s.pp = split_pp(kind, p);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = align_up(off + bytes, 256);
+    return o;
+  };
+  s.off_Ap = take(sizeof(double) * (size_t)m * k * p);
+  s.off_Bp = take(sizeof(double) * (size_t)k * n * p);
+  s.off_Aq = take(sizeof(double) * (size_t)m * k * s.pp);
+  s.off_Bq = take(sizeof(double) * (size_t)k * n * s.pp);
+  s.off_Cq = take(sizeof(double) * (size_t)m * n * s.pp);
+  s.off_Cp = take(sizeof(double) * (size_t)m * n * p);
+  s.total = off;
+  return s;
+}
+
+static int run_split_gemm(int p, const Opts &o, int m, int n, int k, const double *A, int lda,
+                          const double *B, int ldb, double *C, int ldc, void *ws,
+                          cudaStream_t st) {
+  const SplitPlan sp = make_split_plan(p, o.split_kind, m, n, k);
+  char *base = reinterpret_cast<char *>(ws);
+  const double *Ac = A, *Bc = B;
+  if (lda != k && m > 0 && k > 0) {
+    double *Ap = reinterpret_cast<double *>(base + sp.off_Ap);
+    MDG_TRY_CUDA(cudaMemcpy2DAsync(Ap, sizeof(double) * k * p, A, sizeof(double) * lda * p,
+                                   sizeof(double) * k * p, m, cudaMemcpyDeviceToDevice, st));
+    Ac = Ap;
+  }
+  if (ldb != n && k > 0 && n > 0) {
+    double *Bp = reinterpret_cast<double *>(base + sp.off_Bp);
+    MDG_TRY_CUDA(cudaMemcpy2DAsync(Bp, sizeof(double) * n * p, B, sizeof(double) * ldb * p,
+                                   sizeof(double) * n * p, k, cudaMemcpyDeviceToDevice, st));
+    Bc = Bp;
+  }
+  double *Aq = reinterpret_cast<double *>(base + sp.off_Aq);
+  double *Bq = reinterpret_cast<double *>(base + sp.off_Bq);
+  double *Cq = reinterpret_cast<double *>(base + sp.off_Cq);
+  MDG_TRY(launch_split(o.split_kind, o.split_exact, p, (long long)m * k, Ac, Aq, 0, 0, st));
+  MDG_TRY(launch_split(o.split_kind, o.split_exact, p, (long long)k * n, Bc, Bq, 0, 0, st));
+  MDG_TRY(launch_slice_conv(sp.pp, m, n, k, Aq, Bq, Cq, st));
+  double *Cout = (ldc == n) ? C : reinterpret_cast<double *>(base + sp.off_Cp);
+  MDG_TRY(launch_squeeze(p, sp.pp, (long long)m * n, Cq, sp.pp, 1, Cout, st));
+  if (ldc != n && m > 0 && n > 0) {
+    MDG_TRY_CUDA(cudaMemcpy2DAsync(C, sizeof(double) * ldc * p, Cout, sizeof(double) * n * p,
+                                   sizeof(double) * n * p, m, cudaMemcpyDeviceToDevice, st));
+  }
+  return MDG_SUCCESS;
+}
+
+static size_t workspace_bytes(int form, int p, int m, int n, int k, const Opts &o) {
+  if (form == MDG_FORM_PLAIN) return 0;
+  if (form == MDG_FORM_FP64_SPLIT) return make_split_plan(p, o.split_kind, m, n, k).total;
+  return make_slice_plan(p, o.slices, o.diagonals, m, n, k).total;
+}
+
+}  // namespace mdgi
+
+using namespace mdgi;
+
+extern "C" {
+
+const char *mdg_status_string(int status) {
+  switch (status) {
+    case MDG_SUCCESS: return "success";
+    case MDG_ERROR_INVALID_LIMBS: return "invalid limb count (P must be 2, 4, 8 or 16)";
+    case MDG_ERROR_INVALID_SIZE: return "invalid size or leading dimension";
+    case MDG_ERROR_NULL_POINTER: return "null pointer";
+    case MDG_ERROR_INVALID_FORM: return "invalid form or option";
+    case MDG_ERROR_WORKSPACE: return "workspace missing or too small";
+    case MDG_ERROR_CUDA: return "CUDA error";
+    case MDG_ERROR_NOT_SUPPORTED: return "not supported";
+    case MDG_ERROR_TIMEOUT: return "device wait timed out";
+    case MDG_ERROR_ALLOCATION: return "allocation failed";
+  }
+  return "unknown status";
+}
+
+const char *mdg_last_cuda_error(void) { return g_cuda_error; }
+
+int mdg_version(void) { return 100; }
+
+int mdg_default_slices(int p) {
+  switch (p) {
+    case 2: return 14;
+    case 4: return 28;
+    case 8: return 55;
+    case 16: return 108;
+  }
+  return 0;
+}
+
+size_t mdg_gemm_workspace_size(int form, int p, int m, int n, int k, const mdg_options *opt) {
+  Opts o;
+  if (!valid_p(p) || m < 0 || n < 0 || k < 0) return 0;
+  if (resolve_opts(p, opt, &o) != MDG_SUCCESS) return 0;
+  return workspace_bytes(form, p, m, n, k, o);
+}
+
+int mdg_gemm(int form, int p, int m, int n, int k, const double *A, int lda, const double *B,
+             int ldb, double *C, int ldc, const mdg_options *opt, void *workspace,
+             size_t workspace_bytes_, void *stream) {
+  MDG_TRY(check_gemm_args(form, p, m, n, k, A, lda, B, ldb, C, ldc));
+  Opts o;
+  MDG_TRY(resolve_opts(p, opt, &o));
+  cudaStream_t st = as_stream(stream);
+  if (m == 0 || n == 0) return MDG_SUCCESS;
+  if (k == 0) {  // empty sum: C = 0
+    MDG_TRY_CUDA(cudaMemset2DAsync(C, sizeof(double) * ldc * p, 0, sizeof(double) * n * p, m, st));
+    return MDG_SUCCESS;
+  }
+  if (form == MDG_FORM_PLAIN)
+    return launch_plain_gemm(p, m, n, k, A, lda, B, ldb, C, ldc, st);
+  const size_t need = workspace_bytes(form, p, m, n, k, o);
+  if (!workspace || workspace_bytes_ < need) return MDG_ERROR_WORKSPACE;
+  if (form == MDG_FORM_FP64_SPLIT)
+    return run_split_gemm(p, o, m, n, k, A, lda, B, ldb, C, ldc, workspace, st);
+  const SlicePlan pl = make_slice_plan(p, o.slices, o.diagonals, m, n, k);
+  if (pl.Mp > 65535 || pl.Np > 65535) return MDG_ERROR_NOT_SUPPORTED;
+  return run_slice_gemm(pl, A, lda, B, ldb, C, ldc, workspace, default_engine(), st);
+}
+
+int mdg_gemm_host(int form, int p, int m, int n, int k, const double *A, const double *B,
+                  double *C, const mdg_options *opt) {
+  MDG_TRY(check_gemm_args(form, p, m, n, k, A, std::max(k, 1), B, std::max(n, 1), C,
+                          std::max(n, 1)));
+  Opts o;
+  MDG_TRY(resolve_opts(p, opt, &o));
+  if (m == 0 || n == 0) return MDG_SUCCESS;
+  std::lock_guard<std::mutex> lk(g_cache.mu);
+  const size_t sa = sizeof(double) * (size_t)m * k * p, sb = sizeof(double) * (size_t)k * n * p,
+               sc = sizeof(double) * (size_t)m * n * p;
+  void *dA, *dB, *dC, *ws = nullptr;
+  MDG_TRY(g_cache.get(0, sa, &dA));
+  MDG_TRY(g_cache.get(1, sb, &dB));
+  MDG_TRY(g_cache.get(2, sc, &dC));
+  const size_t need = workspace_bytes(form, p, m, n, k, o);
+  if (need) MDG_TRY(g_cache.get(3, need, &ws));
+  cudaStream_t st = 0;
+  if (sa) MDG_TRY_CUDA(cudaMemcpyAsync(dA, A, sa, cudaMemcpyHostToDevice, st));
+  if (sb) MDG_TRY_CUDA(cudaMemcpyAsync(dB, B, sb, cudaMemcpyHostToDevice, st));
+  MDG_TRY(mdg_gemm(form, p, m, n, k, (const double *)dA, std::max(k, 1), (const double *)dB, n,
+                   (double *)dC, n, opt, ws, need, st));
+  MDG_TRY_CUDA(cudaMemcpyAsync(C, dC, sc, cudaMemcpyDeviceToHost, st));
+  MDG_TRY_CUDA(cudaStreamSynchronize(st));
+  return MDG_SUCCESS;
+}
+
+void mdg_release_cache(void) { g_cache.release(); }
+
+// ---------------------------------------------------------------- batched --
+
+size_t mdg_gemm_batched_workspace_size(int form, const mdg_problem *problems, int count,
+                                       const mdg_options *opt) {
+  if (!problems || count < 0) return 0;
+  size_t total = align_up(sizeof(mdg_problem) * (size_t)count, 256) +
+                 align_up(sizeof(int) * (size_t)(count + 1), 256);
+  if (form == MDG_FORM_PLAIN) return total;
+  size_t mx = 0;
+  for (int i = 0; i < count; ++i) {
+    const mdg_problem &q = problems[i];
+    mx = std::max(mx, mdg_gemm_workspace_size(form, q.p, q.m, q.n, q.k, opt));
+  }
+  return total + mx;
+}
+
+int mdg_gemm_batched(int form, const mdg_problem *problems, int count, const mdg_options *opt,
+                     void *workspace, size_t wsb, void *stream) {
+  if (count < 0) return MDG_ERROR_INVALID_SIZE;
+  if (count == 0) return MDG_SUCCESS;
+  if (!problems) return MDG_ERROR_NULL_POINTER;
+  int max_p = 2;
+  for (int i = 0; i < count; ++i) {
+    const mdg_problem &q = problems[i];
+    MDG_TRY(check_gemm_args(form, q.p, q.m, q.n, q.k, q.A, q.lda, q.B, q.ldb, q.C, q.ldc));
+    max_p = std::max(max_p, q.p);
+  }
+  const size_t need = mdg_gemm_batched_workspace_size(form, problems, count, opt);
+  if (!workspace || wsb < need) return MDG_ERROR_WORKSPACE;
+  cudaStream_t st = as_stream(stream);
+  char *base = reinterpret_cast<char *>(workspace);
+  if (form == MDG_FORM_PLAIN) {
+    std::vector<int> starts(count + 1, 0);
+    for (int i = 0; i < count; ++i) {
+      const mdg_problem &q = problems[i];
+      const long long tiles = (q.k == 0) ? 0 : (long long)((q.m + 15) / 16) * ((q.n + 15) / 16);
+      starts[i + 1] = starts[i] + (int)tiles;
+    }
+    for (int i = 0; i < count; ++i)
+      if (problems[i].k == 0 && problems[i].m > 0 && problems[i].n > 0)
+        MDG_TRY_CUDA(cudaMemset2DAsync(problems[i].C, sizeof(double) * problems[i].ldc * problems[i].p,
+                                       0, sizeof(double) * problems[i].n * problems[i].p,
+                                       problems[i].m, st));
+    auto *dprobs = reinterpret_cast<mdg_problem *>(base);
+    auto *dstarts =
+        reinterpret_cast<int *>(base + align_up(sizeof(mdg_problem) * (size_t)count, 256));
+    // the table travels with the launch stream: pinned staging would need a
+    // host allocation, so the copy waits for the host data to be read
+    MDG_TRY_CUDA(cudaMemcpyAsync(dprobs, problems, sizeof(mdg_problem) * count,
+                                 cudaMemcpyHostToDevice, st));
+    MDG_TRY_CUDA(cudaMemcpyAsync(dstarts, starts.data(), sizeof(int) * (count + 1),
+                                 cudaMemcpyHostToDevice, st));
+    MDG_TRY_CUDA(cudaStreamSynchronize(st));
+    return launch_plain_batched(dprobs, count, max_p, dstarts, starts[count], st);
+  }
+  // split forms: the stages of each problem in turn on one stream, sharing
+  // the largest workspace
+  void *ws = base + align_up(sizeof(mdg_problem) * (size_t)count, 256) +
+             align_up(sizeof(int) * (size_t)(count + 1), 256);
+  const size_t wsz = need - (static_cast<char *>(ws) - base);
+  for (int i = 0; i < count; ++i) {
+    const mdg_problem &q = problems[i];
+    MDG_TRY(mdg_gemm(form, q.p, q.m, q.n, q.k, q.A, q.lda, q.B, q.ldb, q.C, q.ldc, opt, ws, wsz,
+                     stream));
+  }
+  return MDG_SUCCESS;
+}
+
+// ------------------------------------------------------- stage entries --
+
+int mdg_split(int kind, int exact, int p, long long count, const double *x, double *out,
+              void *stream) {
+  if (!valid_p(p)) return MDG_ERROR_INVALID_LIMBS;
+  if (kind < 0 || kind > 2 || (exact != 0 && exact != 1)) return MDG_ERROR_INVALID_FORM;
+  if (kind == 2 && p != 2) return MDG_ERROR_INVALID_LIMBS;
+  if (count < 0) return MDG_ERROR_INVALID_SIZE;
+  if (count > 0 && (!x || !out)) return MDG_ERROR_NULL_POINTER;
+  return launch_split(kind, exact, p, count, x, out, 0, 0, as_stream(stream));
+}
+
+int mdg_squeeze(int p, int pp, long long count, const double *x, double *y, void *stream) {
+  if (!valid_p(p)) return MDG_ERROR_INVALID_LIMBS;
+  if (pp < 1 || count < 0) return MDG_ERROR_INVALID_SIZE;
+  if (count > 0 && (!x || !y)) return MDG_ERROR_NULL_POINTER;
+  return launch_squeeze(p, pp, count, x, pp, 1, y, as_stream(stream));
+}
+
+size_t mdg_slice_conv_workspace_size(int pp, int m, int n, int k) {
+  (void)pp; (void)m; (void)n; (void)k;
+  return 0;
+}
+
+int mdg_slice_conv(int pp, int m, int n, int k, const double *Aq, const double *Bq, double *Cq,
+                   void *workspace, size_t workspace_bytes_, void *stream) {
+  (void)workspace;
+  (void)workspace_bytes_;
+  if (pp < 1 || m < 0 || n < 0 || k < 0) return MDG_ERROR_INVALID_SIZE;
+  if ((m > 0 && n > 0 && !Cq) || (m > 0 && k > 0 && !Aq) || (k > 0 && n > 0 && !Bq))
+    return MDG_ERROR_NULL_POINTER;
+  return launch_slice_conv(pp, m, n, k, Aq, Bq, Cq, as_stream(stream));
+}
+
+int mdg_scale_exponents(int p, int m, int n, int k, const double *A, int lda, const double *B,
+                        int ldb, int *E, int *F, void *stream) {
+  if (!valid_p(p)) return MDG_ERROR_INVALID_LIMBS;
+  if (m < 0 || n < 0 || k < 0 || lda < std::max(k, 1) || ldb < std::max(n, 1))
+    return MDG_ERROR_INVALID_SIZE;
+  if ((m > 0 && (!E || (k > 0 && !A))) || (n > 0 && (!F || (k > 0 && !B))))
+    return MDG_ERROR_NULL_POINTER;
+  std::lock_guard<std::mutex> lk(g_cache.mu);
+  void *bits;
+  MDG_TRY(g_cache.get(3, sizeof(unsigned long long) * (size_t)(std::max(m, 1) + std::max(n, 1)),
+                      &bits));
+  auto *rb = reinterpret_cast<unsigned long long *>(bits);
+  return launch_scale_exponents(p, m, n, k, A, lda, B, ldb, rb, rb + std::max(m, 1), E, F,
+                                as_stream(stream));
+}
+
+int mdg_slice_digits(int p, int s, int rows, int cols, const double *X, int ldx, const int *E,
+                     int trans, void *planes, int ld_out, long long plane_stride,
+                     void *stream) {
+  if (!valid_p(p)) return MDG_ERROR_INVALID_LIMBS;
+  if (s < 1 || s > 128 || rows < 0 || cols < 0 || ld_out < cols) return MDG_ERROR_INVALID_SIZE;
+  if (plane_stride < (long long)rows * ld_out) return MDG_ERROR_INVALID_SIZE;
+  if (trans ? (ldx < std::max(rows, 1)) : (ldx < std::max(cols, 1))) return MDG_ERROR_INVALID_SIZE;
+  if (rows > 0 && cols > 0 && (!X || !E || !planes)) return MDG_ERROR_NULL_POINTER;
+  if (rows > 65535) return MDG_ERROR_NOT_SUPPORTED;
+  return launch_digits(p, s, rows, cols, X, ldx, E, trans, planes, ld_out, plane_stride, rows,
+                       cols, as_stream(stream));
+}
+
+int mdg_slice_diagonals(int s, int D, int m, int n, int k, const void *dA, const void *dB, int ld,
+                        long long plane_a, long long plane_b, long long *Cd, void *stream) {
+  if (s < 1 || D < 1 || D > 2 * s - 1 || m < 0 || n < 0 || k < 0) return MDG_ERROR_INVALID_SIZE;
+  if (m % 128 || n % 128 || k % 64 || ld < k) return MDG_ERROR_INVALID_SIZE;
+  if (m == 0 || n == 0) return MDG_SUCCESS;
+  if (!dA || !dB || !Cd) return MDG_ERROR_NULL_POINTER;
+  const long long plane_c = (long long)m * n;
+  if (default_engine() == 1)
+    return launch_diag_gemm_tc(s, D, m, n, k, dA, dB, ld, plane_a, plane_b, Cd, plane_c, n,
+                               as_stream(stream));
+  return launch_diag_gemm_v0(s, D, m, n, k, dA, dB, ld, plane_a, plane_b, Cd, plane_c, n,
+                             as_stream(stream));
+}
+
+int mdg_renorm_diagonals(int p, int D, int m, int n, const long long *Cd, const int *E,
+                         const int *F, double *C, int ldc, void *stream) {
+  if (!valid_p(p)) return MDG_ERROR_INVALID_LIMBS;
+  if (D < 1 || m < 0 || n < 0 || ldc < std::max(n, 1)) return MDG_ERROR_INVALID_SIZE;
+  if (m == 0 || n == 0) return MDG_SUCCESS;
+  if (!Cd || !E || !F || !C) return MDG_ERROR_NULL_POINTER;
+  if (m > 65535) return MDG_ERROR_NOT_SUPPORTED;
+  return launch_renorm(p, D, m, n, Cd, (long long)m * n, n, E, F, C, ldc, as_stream(stream));
+}
+
+}  // extern "C"

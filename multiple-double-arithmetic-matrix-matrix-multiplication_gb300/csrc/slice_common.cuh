@@ -1,0 +1,91 @@
+// Fixed-width two's complement integers in registers, used by the digit
+// split and by the renormalisation of the slice-digit form.  Word 0 is the
+// least significant.  Every loop is unrolled over the compile-time width so
+// that the words stay in registers; positions that vary at run time are
+// handled with predicated selects instead of indexed accesses.
+#pragma once
+
+#include <stdint.h>
+
+namespace mdgi {
+
+// w += v * 2^q for q >= 0 (v sign-extended).
+template <int NW>
+__device__ __forceinline__ void wide_add_shifted(uint64_t (&w)[NW], int64_t v, int q) {
+  const int qw = q >> 6, r = q & 63;
+  const uint64_t fill = (uint64_t)(v >> 63);
+  const uint64_t lo = (uint64_t)v << r;
+  const uint64_t hi = r ? (uint64_t)(v >> (64 - r)) : fill;
+  uint64_t carry = 0;
+#pragma unroll
+  for (int i = 0; i < NW; ++i) {
+    const uint64_t add = (i < qw) ? 0ull : (i == qw) ? lo : (i == qw + 1) ? hi : fill;
+    const uint64_t s = w[i] + add;
+    const uint64_t c1 = s < add;
+    const uint64_t s2 = s + carry;
+    const uint64_t c2 = s2 < s;
+    w[i] = s2;
+    carry = c1 | c2;
+  }
+}
+
+// The 64 bits of w starting at bit pos (0 <= pos < 64 NW); bits above the
+// top word read as the sign.
+template <int NW>
+__device__ __forceinline__ uint64_t wide_bits64(const uint64_t (&w)[NW], int pos) {
+  const int qw = pos >> 6, r = pos & 63;
+  const uint64_t fill = (uint64_t)((int64_t)w[NW - 1] >> 63);
+  uint64_t lo = fill, hi = fill;
+#pragma unroll
+  for (int i = 0; i < NW; ++i) {
+    if (i == qw) lo = w[i];
+    if (i == qw + 1) hi = w[i];
+  }
+  return r ? ((lo >> r) | (hi << (64 - r))) : lo;
+}
+
+// Index of the highest set bit of a non-negative w, -1 for zero.
+template <int NW>
+__device__ __forceinline__ int wide_msb(const uint64_t (&w)[NW]) {
+  int t = -1;
+#pragma unroll
+  for (int i = 0; i < NW; ++i)
+    if (w[i]) t = i * 64 + 63 - __clzll((long long)w[i]);
+  return t;
+}
+
+// Any bit set strictly below position pos (pos >= 0)?
+template <int NW>
+__device__ __forceinline__ bool wide_any_below(const uint64_t (&w)[NW], int pos) {
+  const int qw = pos >> 6, r = pos & 63;
+  uint64_t acc = 0;
+#pragma unroll
+  for (int i = 0; i < NW; ++i) {
+    if (i < qw) acc |= w[i];
+    if (i == qw && r) acc |= w[i] & ((1ull << r) - 1);
+  }
+  return acc != 0;
+}
+
+template <int NW>
+__device__ __forceinline__ void wide_neg(uint64_t (&w)[NW]) {
+  uint64_t carry = 1;
+#pragma unroll
+  for (int i = 0; i < NW; ++i) {
+    const uint64_t s = ~w[i] + carry;
+    carry = (carry && s == 0) ? 1 : 0;
+    w[i] = s;
+  }
+}
+
+// Scale exponent of a row / column from the largest sum of absolute limbs
+// M: the frexp exponent of M, plus one when M lies within 2^-29 of 2^e.
+__device__ __forceinline__ int scale_exp(double M) {
+  if (!(M > 0.0)) return 0;
+  int e;
+  frexp(M, &e);
+  if (M > ldexp(1.0 - ldexp(1.0, -29), e)) e += 1;
+  return e;
+}
+
+}  // namespace mdgi

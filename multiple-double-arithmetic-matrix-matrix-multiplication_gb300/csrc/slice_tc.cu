@@ -1,0 +1,447 @@
+// The slice-digit form of the multi-double GEMM: split, diagonal GEMM on
+// BF16 tensor cores, renormalisation.
+//
+// 1. scale exponents.  E[r] for each row of A and F[c] for each column of B
+//    from the largest sum of absolute limbs; 2^E bounds every entry.
+// 2. digits.  Each P-double a of row r becomes the integer
+//       V = sum_l floor(a_l * 2^(S - E[r])),  S = 7 + 8 (s - 1),
+//    written as s balanced base-256 digits d_0 (most significant) ..
+//    d_{s-1} in [-128, 128].  Digit i of every entry forms one BF16 plane
+//    (the integers up to 256 are exact in BF16).  A's planes are m x k,
+//    B's are transposed to n x k so both operands are K-major.
+// 3. diagonal GEMM.  C_d = sum_{i+j=d} A_i B_j^T for d < D.  One product
+//    of two digits is at most 2^14, so an FP32 accumulator holds the exact
+//    sum of 256 of them (|sum| <= 2^22); every 256 products the FP32
+//    accumulator is flushed into 64-bit integers.  All sums are exact.
+// 4. renormalisation.  W = sum_d C_d 256^(D-1-d) is formed exactly in
+//    wide integers and rounded to P limbs, each to nearest, scaled by
+//    2^(E[r] + F[c] - 14 - 8 (D - 1)).
+// The reference has no counterpart of steps 1-4; its split form cuts limbs
+// into FP64 slices for FP64 DMMA (floatybits.cu, TCtest.cu).  The oracle's
+// section 8 restates these steps on the CPU, and the GPU result equals it
+// bit for bit.
+#include "common.cuh"
+#include "slice_common.cuh"
+#include "slice_tc.cuh"
+
+#include <cuda_bf16.h>
+
+namespace {
+
+using mdgi::wide_add_shifted;
+
+// ------------------------------------------------------------ exponents --
+// Block 32 x 8 covers 32 columns x 256 rows; each warp walks 32 rows of
+// one 32-column strip.  Row maxima: warp reduction, one atomic per row per
+// warp.  Column maxima: one atomic per thread.  Maxima of non-negative
+// doubles are compared as 64-bit integers.
+__global__ void absmax_kernel(int P, int R, int Cn, const double *__restrict__ X, int ldx,
+                              unsigned long long *rowbits, unsigned long long *colbits) {
+  const int c = blockIdx.x * 32 + threadIdx.x;
+  const int r0 = blockIdx.y * 256 + threadIdx.y * 32;
+  double cm = 0.0;
+  for (int rr = 0; rr < 32; ++rr) {
+    const int r = r0 + rr;
+    if (r >= R) break;
+    double v = 0.0;
+    if (c < Cn) {
+      const double *x = X + ((size_t)r * ldx + c) * P;
+      v = fabs(x[0]);
+      for (int l = 1; l < P; ++l) v = v + fabs(x[l]);
+    }
+    cm = fmax(cm, v);
+    if (rowbits) {
+      double w = v;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) w = fmax(w, __shfl_xor_sync(0xffffffffu, w, o));
+      if (threadIdx.x == 0) atomicMax(rowbits + r, (unsigned long long)__double_as_longlong(w));
+    }
+  }
+  if (colbits && c < Cn) atomicMax(colbits + c, (unsigned long long)__double_as_longlong(cm));
+}
+
+__global__ void exps_kernel(int count, const unsigned long long *__restrict__ bits,
+                            int *__restrict__ E) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) E[i] = mdgi::scale_exp(__longlong_as_double((long long)bits[i]));
+}
+
+// --------------------------------------------------------------- digits --
+// One thread per element of the padded plane (prow, pcol); pcol (the k
+// index) is the fastest, so plane stores are coalesced.  Outside the valid
+// region every digit is zero.
+template <int NW>
+__global__ void digits_kernel(int P, int s, int rows, int cols, const double *__restrict__ X,
+                              int ldx, const int *__restrict__ E, int trans,
+                              __nv_bfloat16 *__restrict__ planes, int ld_out,
+                              long long plane_stride, int rows_pad, int cols_pad) {
+  const int pc = blockIdx.x * blockDim.x + threadIdx.x;
+  const int pr = blockIdx.y;
+  if (pc >= cols_pad || pr >= rows_pad) return;
+  __nv_bfloat16 *out = planes + (size_t)pr * ld_out + pc;
+  if (pr >= rows || pc >= cols) {
+    for (int i = 0; i < s; ++i) out[i * plane_stride] = __float2bfloat16_rn(0.0f);
+    return;
+  }
+  const double *a = trans ? X + ((size_t)pc * ldx + pr) * P : X + ((size_t)pr * ldx + pc) * P;
+  const int S = 7 + 8 * (s - 1);
+  const int Er = E[pr];
+  uint64_t w[NW];
+#pragma unroll
+  for (int i = 0; i < NW; ++i) w[i] = 0;
+  for (int l = 0; l < P; ++l) {
+    const double x = a[l];
+    if (x == 0.0) continue;
+    int e;
+    const double f = frexp(x, &e);
+    const int64_t m = (int64_t)ldexp(f, 53);
+    const int q = e - 53 + S - Er;
+    if (q >= 0) {
+      wide_add_shifted<NW>(w, m, q);
+    } else if (q > -64) {
+      wide_add_shifted<NW>(w, m >> (-q), 0);
+    } else {
+      wide_add_shifted<NW>(w, m < 0 ? -1 : 0, 0);
+    }
+  }
+  // balanced digits from the bottom: t = byte + carry, t >= 128 -> t - 256
+  int carry = 0;
+#pragma unroll
+  for (int wi = 0; wi < NW; ++wi) {
+    const uint64_t word = w[wi];
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int p = wi * 8 + b;
+      if (p < s - 1) {
+        const int t = (int)((word >> (8 * b)) & 255) + carry;
+        const int d = t >= 128 ? t - 256 : t;
+        carry = t >= 128 ? 1 : 0;
+        out[(s - 1 - p) * plane_stride] = __float2bfloat16_rn((float)d);
+      }
+    }
+  }
+  const int top = (int)(int64_t)mdgi::wide_bits64<NW>(w, 8 * (s - 1)) + carry;
+  out[0] = __float2bfloat16_rn((float)top);
+}
+
+// ---------------------------------------------------- diagonal GEMM v0 --
+// mma.sync m16n8k16 BF16 -> FP32.  Block 128 x 64, 8 warps as 4 x 2, warp
+// tile 32 x 32 (2 x 4 MMA tiles), K chunk 32 through shared memory.
+constexpr int BM = 128, BN = 64, BK = 32, SK = BK + 8;
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4],
+                                         const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// x is an integer-valued float with |x| <= 2^22: adding 1.5 * 2^23 puts it
+// in the significand exactly; the bits minus those of 1.5 * 2^23 are x.
+__device__ __forceinline__ int64_t exact_int(float x) {
+  return (int64_t)(__float_as_int(x + 12582912.0f) - 0x4B400000);
+}
+
+__global__ void __launch_bounds__(256)
+    diag_gemm_v0(int s, int D, int Kp, const __nv_bfloat16 *__restrict__ dA,
+                 const __nv_bfloat16 *__restrict__ dB, int ld, long long plane_a,
+                 long long plane_b, long long *__restrict__ Cd, long long plane_c, int ldc) {
+  __shared__ __align__(16) __nv_bfloat16 As[BM][SK];
+  __shared__ __align__(16) __nv_bfloat16 Bs[BN][SK];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, t = lane & 3;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int row0 = blockIdx.y * BM, col0 = blockIdx.x * BN;
+
+  for (int d = 0; d < D; ++d) {
+    float acc[2][4][4];
+    int64_t tot[2][4][4];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          acc[a][b][c] = 0.f;
+          tot[a][b][c] = 0;
+        }
+    int terms = 0;
+    const int ilo = max(0, d - (s - 1)), ihi = min(d, s - 1);
+    for (int i = ilo; i <= ihi; ++i) {
+      const __nv_bfloat16 *Ai = dA + i * plane_a + (size_t)row0 * ld;
+      const __nv_bfloat16 *Bj = dB + (d - i) * plane_b + (size_t)col0 * ld;
+      for (int k0 = 0; k0 < Kp; k0 += BK) {
+        // A: 128 x 32 = 512 vectors of 8; B: 64 x 32 = 256 vectors
+#pragma unroll
+        for (int v = tid; v < BM * BK / 8; v += 256) {
+          const int r = v >> 2, cc = (v & 3) * 8;
+          *reinterpret_cast<uint4 *>(&As[r][cc]) =
+              *reinterpret_cast<const uint4 *>(Ai + (size_t)r * ld + k0 + cc);
+        }
+        {
+          const int r = tid >> 2, cc = (tid & 3) * 8;
+          *reinterpret_cast<uint4 *>(&Bs[r][cc]) =
+              *reinterpret_cast<const uint4 *>(Bj + (size_t)r * ld + k0 + cc);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; kk += 16) {
+          uint32_t af[2][4], bf[4][2];
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt) {
+            const int r = wm + mt * 16 + g;
+            af[mt][0] = *reinterpret_cast<const uint32_t *>(&As[r][kk + 2 * t]);
+            af[mt][1] = *reinterpret_cast<const uint32_t *>(&As[r + 8][kk + 2 * t]);
+            af[mt][2] = *reinterpret_cast<const uint32_t *>(&As[r][kk + 8 + 2 * t]);
+            af[mt][3] = *reinterpret_cast<const uint32_t *>(&As[r + 8][kk + 8 + 2 * t]);
+          }
+#pragma unroll
+          for (int nt = 0; nt < 4; ++nt) {
+            const int c = wn + nt * 8 + g;
+            bf[nt][0] = *reinterpret_cast<const uint32_t *>(&Bs[c][kk + 2 * t]);
+            bf[nt][1] = *reinterpret_cast<const uint32_t *>(&Bs[c][kk + 8 + 2 * t]);
+          }
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) mma_bf16(acc[mt][nt], af[mt], bf[nt]);
+        }
+        __syncthreads();
+        terms += BK;
+        if (terms == 256) {
+#pragma unroll
+          for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b)
+#pragma unroll
+              for (int c = 0; c < 4; ++c) {
+                tot[a][b][c] += exact_int(acc[a][b][c]);
+                acc[a][b][c] = 0.f;
+              }
+          terms = 0;
+        }
+      }
+    }
+    long long *out = Cd + d * plane_c;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int r = row0 + wm + mt * 16 + g + h * 8;
+          const int c = col0 + wn + nt * 8 + 2 * t;
+          const long long v0 = tot[mt][nt][2 * h] + exact_int(acc[mt][nt][2 * h]);
+          const long long v1 = tot[mt][nt][2 * h + 1] + exact_int(acc[mt][nt][2 * h + 1]);
+          *reinterpret_cast<longlong2 *>(out + (size_t)r * ldc + c) = make_longlong2(v0, v1);
+        }
+  }
+}
+
+// --------------------------------------------------------------- renorm --
+template <int P, int NW>
+__global__ void renorm_kernel(int D, int m, int n, const long long *__restrict__ Cd,
+                              long long plane_c, int ldcd, const int *__restrict__ E,
+                              const int *__restrict__ F, double *__restrict__ C, int ldc) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (c >= n || r >= m) return;
+  uint64_t w[NW];
+#pragma unroll
+  for (int i = 0; i < NW; ++i) w[i] = 0;
+  const long long *src = Cd + (size_t)r * ldcd + c;
+  for (int d = 0; d < D; ++d) {
+    const long long v = src[d * plane_c];
+    if (v) wide_add_shifted<NW>(w, v, 8 * (D - 1 - d));
+  }
+  const int scale = E[r] + F[c] - 14 - 8 * (D - 1);
+  double *out = C + ((size_t)r * ldc + c) * P;
+#pragma unroll 1
+  for (int l = 0; l < P; ++l) {
+    const bool neg = (int64_t)w[NW - 1] < 0;
+    uint64_t mag[NW];
+#pragma unroll
+    for (int i = 0; i < NW; ++i) mag[i] = w[i];
+    if (neg) mdgi::wide_neg<NW>(mag);
+    const int tb = mdgi::wide_msb<NW>(mag);
+    if (tb < 0) {
+      out[l] = 0.0;
+      continue;
+    }
+    const int sh = tb > 52 ? tb - 52 : 0;
+    uint64_t mm = mdgi::wide_bits64<NW>(mag, sh) & ((1ull << 53) - 1);
+    if (sh > 0) {
+      const bool rb = (mdgi::wide_bits64<NW>(mag, sh - 1) & 1ull) != 0;
+      const bool sticky = sh > 1 && mdgi::wide_any_below<NW>(mag, sh - 1);
+      if (rb && (sticky || (mm & 1))) mm += 1;
+    }
+    const double v = ldexp((double)mm, sh + scale);
+    out[l] = neg ? -v : v;
+    wide_add_shifted<NW>(w, neg ? (int64_t)mm : -(int64_t)mm, sh);
+  }
+}
+
+}  // namespace
+
+namespace mdgi {
+
+int words_for(int s, int D) {
+  // digits need S + 2 bits plus a word of headroom; W needs 8 (D - 1) + 64
+  const int bits = std::max(7 + 8 * (s - 1) + 2, 8 * (D - 1) + 72);
+  const int w = (bits + 63) / 64 + 1;
+  if (w <= 4) return 4;
+  if (w <= 6) return 6;
+  if (w <= 10) return 10;
+  if (w <= 16) return 16;
+  return 0;
+}
+
+SlicePlan make_slice_plan(int p, int s, int D, int m, int n, int k) {
+  SlicePlan pl{};
+  pl.p = p;
+  pl.s = s;
+  pl.D = D;
+  pl.m = m;
+  pl.n = n;
+  pl.k = k;
+  pl.Mp = (int)align_up(std::max(m, 1), 128);
+  pl.Np = (int)align_up(std::max(n, 1), 128);
+  pl.Kp = (int)align_up(std::max(k, 1), 64);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = align_up(off + bytes, 256);
+    return o;
+  };
+  pl.off_rowbits = take(sizeof(unsigned long long) * pl.Mp);
+  pl.off_colbits = take(sizeof(unsigned long long) * pl.Np);
+  pl.off_E = take(sizeof(int) * pl.Mp);
+  pl.off_F = take(sizeof(int) * pl.Np);
+  pl.plane_a = (long long)pl.Mp * pl.Kp;
+  pl.plane_b = (long long)pl.Np * pl.Kp;
+  pl.plane_c = (long long)pl.Mp * pl.Np;
+  pl.off_dA = take(sizeof(__nv_bfloat16) * (size_t)s * pl.plane_a);
+  pl.off_dB = take(sizeof(__nv_bfloat16) * (size_t)s * pl.plane_b);
+  pl.off_Cd = take(sizeof(long long) * (size_t)D * pl.plane_c);
+  pl.total = off;
+  return pl;
+}
+
+int launch_scale_exponents(int p, int m, int n, int k, const double *A, int lda,
+                           const double *B, int ldb, unsigned long long *rowbits,
+                           unsigned long long *colbits, int *E, int *F, cudaStream_t st) {
+  MDG_TRY_CUDA(cudaMemsetAsync(rowbits, 0, sizeof(unsigned long long) * std::max(m, 1), st));
+  MDG_TRY_CUDA(cudaMemsetAsync(colbits, 0, sizeof(unsigned long long) * std::max(n, 1), st));
+  if (k > 0 && m > 0) {
+    dim3 grid(ceil_div(k, 32), ceil_div(m, 256));
+    absmax_kernel<<<grid, dim3(32, 8), 0, st>>>(p, m, k, A, lda, rowbits, nullptr);
+    MDG_TRY_LAUNCH();
+  }
+  if (k > 0 && n > 0) {
+    dim3 grid(ceil_div(n, 32), ceil_div(k, 256));
+    absmax_kernel<<<grid, dim3(32, 8), 0, st>>>(p, k, n, B, ldb, nullptr, colbits);
+    MDG_TRY_LAUNCH();
+  }
+  if (m > 0) {
+    exps_kernel<<<ceil_div(m, 256), 256, 0, st>>>(m, rowbits, E);
+    MDG_TRY_LAUNCH();
+  }
+  if (n > 0) {
+    exps_kernel<<<ceil_div(n, 256), 256, 0, st>>>(n, colbits, F);
+    MDG_TRY_LAUNCH();
+  }
+  return MDG_SUCCESS;
+}
+
+int launch_digits(int p, int s, int rows, int cols, const double *X, int ldx, const int *E,
+                  int trans, void *planes, int ld_out, long long plane_stride, int rows_pad,
+                  int cols_pad, cudaStream_t st) {
+  const int NW = words_for(s, 1);
+  if (!NW) return MDG_ERROR_NOT_SUPPORTED;
+  if (rows_pad == 0 || cols_pad == 0) return MDG_SUCCESS;
+  dim3 grid(ceil_div(cols_pad, 128), rows_pad);
+  auto *pl = reinterpret_cast<__nv_bfloat16 *>(planes);
+#define MDG_DIGITS(W)                                                                    \
+  digits_kernel<W><<<grid, 128, 0, st>>>(p, s, rows, cols, X, ldx, E, trans, pl, ld_out, \
+                                          plane_stride, rows_pad, cols_pad)
+  switch (NW) {
+    case 4: MDG_DIGITS(4); break;
+    case 6: MDG_DIGITS(6); break;
+    case 10: MDG_DIGITS(10); break;
+    default: MDG_DIGITS(16); break;
+  }
+#undef MDG_DIGITS
+  MDG_TRY_LAUNCH();
+  return MDG_SUCCESS;
+}
+
+int launch_diag_gemm_v0(int s, int D, int Mp, int Np, int Kp, const void *dA, const void *dB,
+                        int ld, long long plane_a, long long plane_b, long long *Cd,
+                        long long plane_c, int ldc, cudaStream_t st) {
+  if (Mp % BM || Np % BN || Kp % BK) return MDG_ERROR_INVALID_SIZE;
+  dim3 grid(Np / BN, Mp / BM);
+  diag_gemm_v0<<<grid, 256, 0, st>>>(s, D, Kp, reinterpret_cast<const __nv_bfloat16 *>(dA),
+                                     reinterpret_cast<const __nv_bfloat16 *>(dB), ld, plane_a,
+                                     plane_b, Cd, plane_c, ldc);
+  MDG_TRY_LAUNCH();
+  return MDG_SUCCESS;
+}
+
+int launch_renorm(int p, int D, int m, int n, const long long *Cd, long long plane_c, int ldcd,
+                  const int *E, const int *F, double *C, int ldc, cudaStream_t st) {
+  if (m == 0 || n == 0) return MDG_SUCCESS;
+  const int NW = words_for(1, D);
+  if (!NW) return MDG_ERROR_NOT_SUPPORTED;
+  dim3 grid(ceil_div(n, 128), m);
+#define MDG_RENORM(PP, W)                                                                  \
+  renorm_kernel<PP, W><<<grid, 128, 0, st>>>(D, m, n, Cd, plane_c, ldcd, E, F, C, ldc)
+#define MDG_RENORM_P(PP)           \
+  switch (NW) {                    \
+    case 4: MDG_RENORM(PP, 4); break;  \
+    case 6: MDG_RENORM(PP, 6); break;  \
+    case 10: MDG_RENORM(PP, 10); break; \
+    default: MDG_RENORM(PP, 16); break; \
+  }
+  switch (p) {
+    case 2: MDG_RENORM_P(2); break;
+    case 4: MDG_RENORM_P(4); break;
+    case 8: MDG_RENORM_P(8); break;
+    case 16: MDG_RENORM_P(16); break;
+    default: return MDG_ERROR_INVALID_LIMBS;
+  }
+#undef MDG_RENORM_P
+#undef MDG_RENORM
+  MDG_TRY_LAUNCH();
+  return MDG_SUCCESS;
+}
+
+int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *B, int ldb,
+                   double *C, int ldc, void *ws, int engine, cudaStream_t st) {
+  char *base = reinterpret_cast<char *>(ws);
+  auto *rowbits = reinterpret_cast<unsigned long long *>(base + pl.off_rowbits);
+  auto *colbits = reinterpret_cast<unsigned long long *>(base + pl.off_colbits);
+  int *E = reinterpret_cast<int *>(base + pl.off_E);
+  int *F = reinterpret_cast<int *>(base + pl.off_F);
+  void *dA = base + pl.off_dA;
+  void *dB = base + pl.off_dB;
+  auto *Cd = reinterpret_cast<long long *>(base + pl.off_Cd);
+  MDG_TRY(launch_scale_exponents(pl.p, pl.m, pl.n, pl.k, A, lda, B, ldb, rowbits, colbits, E, F,
+                                 st));
+  MDG_TRY(launch_digits(pl.p, pl.s, pl.m, pl.k, A, lda, E, 0, dA, pl.Kp, pl.plane_a, pl.Mp,
+                        pl.Kp, st));
+  MDG_TRY(launch_digits(pl.p, pl.s, pl.n, pl.k, B, ldb, F, 1, dB, pl.Kp, pl.plane_b, pl.Np,
+                        pl.Kp, st));
+  if (engine == 1) {
+    MDG_TRY(launch_diag_gemm_tc(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
+                                pl.plane_b, Cd, pl.plane_c, pl.Np, st));
+  } else {
+    MDG_TRY(launch_diag_gemm_v0(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
+                                pl.plane_b, Cd, pl.plane_c, pl.Np, st));
+  }
+  MDG_TRY(launch_renorm(pl.p, pl.D, pl.m, pl.n, Cd, pl.plane_c, pl.Np, E, F, C, ldc, st));
+  return MDG_SUCCESS;
+}
+
+}  // namespace mdgi

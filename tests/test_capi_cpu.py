@@ -1,0 +1,77 @@
+"""C ABI checks that need no GPU: the library loads, exports every function
+include/mdgemm.h declares, and rejects bad arguments before any CUDA call."""
+import ctypes
+import re
+
+import pytest
+
+from conftest import pkg
+
+
+@pytest.fixture(scope="module")
+def L():
+    return pkg("_lib").lib()
+
+
+def declared_functions():
+    src = open(pkg("_lib").HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mdg_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_every_declared_symbol_is_exported(L):
+    names = declared_functions()
+    assert len(names) >= 17
+    for name in names:
+        assert hasattr(L, name), name
+    assert set(names) == set(pkg("_lib").SIGNATURES), "ctypes table out of sync with header"
+
+
+def test_status_strings(L):
+    assert L.mdg_status_string(0) == b"success"
+    assert b"limb" in L.mdg_status_string(1)
+    assert L.mdg_status_string(12345) == b"unknown status"
+    assert L.mdg_version() >= 100
+
+
+def test_default_slices(L):
+    assert [L.mdg_default_slices(p) for p in (2, 4, 8, 16)] == [14, 28, 55, 108]
+    assert L.mdg_default_slices(3) == 0
+
+
+@pytest.mark.parametrize("p", [0, 1, 3, 5, 32, -2])
+def test_bad_limb_count_rejected(L, p):
+    assert L.mdg_gemm(0, p, 4, 4, 4, None, 4, None, 4, None, 4, None, None, 0, None) == 1
+    assert L.mdg_split(0, 0, p, 4, None, None, None) == 1
+    assert L.mdg_squeeze(p, 8, 4, None, None, None) == 1
+
+
+def test_bad_sizes_and_pointers_rejected(L):
+    one = ctypes.c_void_p(1)
+    assert L.mdg_gemm(0, 4, -1, 4, 4, one, 4, one, 4, one, 4, None, None, 0, None) == 2
+    assert L.mdg_gemm(0, 4, 4, 4, 8, one, 4, one, 4, one, 4, None, None, 0, None) == 2  # lda < k
+    assert L.mdg_gemm(0, 4, 4, 4, 4, None, 4, one, 4, one, 4, None, None, 0, None) == 3
+    assert L.mdg_gemm(7, 4, 4, 4, 4, one, 4, one, 4, one, 4, None, None, 0, None) == 4
+    assert L.mdg_gemm(1, 4, 4, 4, 4, one, 4, one, 4, one, 4, None, None, 0, None) == 5  # no workspace
+    assert L.mdg_gemm(2, 4, 4, 4, 4, one, 4, one, 4, one, 4, None, None, 0, None) == 5
+    assert L.mdg_split(2, 0, 4, 4, one, one, None) == 1   # mixed split needs P = 2
+    assert L.mdg_split(0, 3, 4, 4, one, one, None) == 4
+    assert L.mdg_squeeze(4, 0, 4, one, one, None) == 2
+    assert L.mdg_slice_diagonals(4, 4, 100, 128, 64, one, one, 64, 1, 1, one, None) == 2
+
+
+def test_empty_problems_succeed_without_gpu(L):
+    assert L.mdg_gemm(0, 4, 0, 5, 5, None, 5, None, 5, None, 5, None, None, 0, None) == 0
+    assert L.mdg_split(0, 0, 4, 0, None, None, None) == 0
+    assert L.mdg_squeeze(4, 16, 0, None, None, None) == 0
+
+
+def test_workspace_sizes(L):
+    api = pkg("api")
+    assert api.workspace_size("plain", 4, 64, 64, 64) == 0
+    ws_split = api.workspace_size("fp64split", 4, 64, 64, 64)
+    assert ws_split >= 16 * 3 * 64 * 64 * 8
+    ws_tc = api.workspace_size("slice_bf16", 4, 64, 64, 64)
+    # digits of A and B (28 planes of 128 x 64 BF16) + 28 diagonal planes
+    assert ws_tc >= 2 * 28 * 128 * 64 * 2 + 28 * 128 * 128 * 8
+    assert api.workspace_size("slice_bf16", 4, 64, 64, 64, slices=200) == 0

@@ -1,0 +1,286 @@
+"""GPU parity: every stage and every form through the C ABI against the
+oracle (and, through the golden files, against the reference itself).
+
+Tolerances: the plain form, the floatybits split, the squeeze and every
+stage of the slice-digit form are bit-exact (compared with ==, NaN-free
+inputs).  The FP64 DMMA slice convolution rounds its FP64 sums in the
+tensor core's own order; it must agree with the oracle's sequential sum to
+2^-50 relative to sum |a||b| per entry, and the whole FP64-split GEMM must
+reach the oracle's error bits within 2 bits.  The slice-digit form must
+reach at least the plain form's normwise error bits minus 1 against the
+exact product.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN, pkg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def api():
+    if not torch.cuda.is_available():
+        pytest.fail("a GPU test ran without a GPU")
+    return pkg("api")
+
+
+def dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def host(t):
+    return t.cpu().numpy()
+
+
+SHAPES = [(1, 1, 1), (7, 5, 3), (31, 33, 17), (33, 31, 64), (64, 64, 64), (16, 48, 129)]
+
+
+# ------------------------------------------------------------------ plain --
+
+@pytest.mark.parametrize("P", [2, 4, 8, 16])
+@pytest.mark.parametrize("shape", SHAPES)
+def test_plain_bit_exact(api, orc, inputs, P, shape):
+    m, n, k = shape
+    if P == 16 and m * n * k > 40000:
+        pytest.skip("hd oracle cost")
+    rng = np.random.default_rng(m * 1000 + n * 10 + k + P)
+    A = inputs.uniform_pd(rng, (m, k), P)
+    B = inputs.uniform_pd(rng, (k, n), P)
+    C = host(api.gemm(dev(A), dev(B), "plain"))
+    assert np.array_equal(C, orc.gemm_plain(P, A, B, m, n, k))
+
+
+@pytest.mark.parametrize("P", [2, 4, 8, 16])
+def test_plain_matches_reference_golden(api, P):
+    g = np.load(os.path.join(GOLDEN, f"matmul_P{P}.npz"))
+    C = host(api.gemm(dev(g["A"]), dev(g["B"]), "plain"))
+    assert np.array_equal(C, g["C"], equal_nan=True)
+
+
+def test_plain_dd64_workload_matches_reference(api):
+    g = np.load(os.path.join(GOLDEN, "matmul_dd64.npz"))
+    C = host(api.gemm(dev(g["A"]), dev(g["B"]), "plain"))
+    assert np.array_equal(C, g["C"])
+
+
+def test_matmulTCnt_mirror(api, inputs, orc):
+    P, A, B = inputs.workload("qd1024", 40, 40, 40)
+    C, t = api.matmulTCnt(A.ravel(), B.ravel(), 40, 32, P, loop_ct=2)
+    assert t > 0
+    assert np.array_equal(C.reshape(40, 40, P), orc.gemm_plain(P, A, B, 40, 40, 40))
+
+
+def test_plain_batched_mixed(api, orc, inputs):
+    probs, rng = inputs.batched_problems(12, seed=5)
+    probs = [(P, m // 8, n // 8, k // 8) for P, m, n, k in probs]
+    ops = inputs.batched_operands(probs, rng)
+    Cs = api.gemm_batched([(dev(A), dev(B)) for A, B in ops], "plain")
+    for (P, m, n, k), (A, B), C in zip(probs, ops, Cs):
+        assert np.array_equal(host(C), orc.gemm_plain(P, A, B, m, n, k))
+
+
+# ---------------------------------------------------------- FP64 split --
+
+@pytest.mark.parametrize("P", [2, 4, 8, 16])
+@pytest.mark.parametrize("kind", ["split4", "split8"])
+@pytest.mark.parametrize("style", ["", "_refstyle"])
+def test_split_matches_reference_golden(api, P, kind, style):
+    g = np.load(os.path.join(GOLDEN, f"{kind}_P{P}{style}.npz"))
+    fn = api.split4pd if kind == "split4" else api.split8pd
+    out = host(fn(g["x"], P))
+    assert np.array_equal(out, g["out"])
+    assert np.array_equal(np.signbit(out), np.signbit(g["out"]))
+
+
+def test_mixsplit_matches_reference_golden(api):
+    g = np.load(os.path.join(GOLDEN, "split_mix_P2.npz"))
+    out = host(api.mixsplit2(g["x"]))
+    assert np.array_equal(out, g["out"]) and np.array_equal(np.signbit(out), np.signbit(g["out"]))
+
+
+@pytest.mark.parametrize("P", [2, 4, 8])
+@pytest.mark.parametrize("kind", ["split4", "split8"])
+def test_exact_split_matches_oracle(api, orc, inputs, P, kind):
+    rng = np.random.default_rng(P)
+    x = inputs.uniform_pd(rng, (300,), P)
+    fn = api.split4pd if kind == "split4" else api.split8pd
+    out = host(fn(x, P, exact=True))
+    ref = orc.split(kind, P, x, exact=True)
+    assert np.array_equal(out, ref) and np.array_equal(np.signbit(out), np.signbit(ref))
+    # exact slices sum back to the limbs
+    pp = ref.shape[1]
+    per = pp // P
+    assert np.array_equal(out.reshape(300, P, per).sum(axis=2), x)
+
+
+@pytest.mark.parametrize("P,pp", [(2, 8), (2, 16), (4, 16), (4, 32), (8, 32), (8, 64),
+                                  (16, 64), (16, 128)])
+def test_squeeze_matches_reference_golden(api, P, pp):
+    g = np.load(os.path.join(GOLDEN, f"squeeze_P{P}_pp{pp}.npz"))
+    assert np.array_equal(host(api.pllsqueeze_old(g["x"], P, pp)), g["y"])
+
+
+@pytest.mark.parametrize("pp,shape", [(16, (8, 8, 8)), (16, (33, 17, 40)), (8, (64, 64, 64)),
+                                      (12, (20, 9, 31))])
+def test_slice_conv_against_oracle(api, orc, inputs, pp, shape):
+    m, n, k = shape
+    P = {16: 4, 8: 2, 12: 2}[pp]
+    kind = {16: "split4", 8: "split4", 12: "mix"}[pp]
+    rng = np.random.default_rng(pp + m)
+    A = inputs.uniform_pd(rng, (m, k), P)
+    B = inputs.uniform_pd(rng, (k, n), P)
+    Aq = orc.split(kind, P, A.reshape(-1, P), exact=True).reshape(m, k, pp)
+    Bq = orc.split(kind, P, B.reshape(-1, P), exact=True).reshape(k, n, pp)
+    got = host(api.slice_conv(dev(Aq), dev(Bq)))
+    ref = orc.slice_conv(pp, Aq, Bq, m, n, k)
+    # |a||b| bound per entry and diagonal
+    absC = orc.slice_conv(pp, np.abs(Aq), np.abs(Bq), m, n, k)
+    assert np.all(np.abs(got - ref) <= 2.0 ** -50 * absC + 1e-300)
+    frac_exact = np.mean(got == ref)
+    print(f"slice_conv pp={pp} {shape}: {frac_exact:.4f} of entries bit-exact")
+
+
+@pytest.mark.parametrize("name,P", [("dd64", 2), ("qd1024", 4)])
+def test_fp64split_error_bits(api, orc, inputs, name, P):
+    import oracle.exact as ex
+    _, A, B = inputs.workload(name, 24, 24, 24)
+    C = host(api.gemm(dev(A), dev(B), "fp64split"))
+    ref = orc.gemm_fp64split(P, A, B, 24, 24, 24)
+    bits = ex.error_bits(C, A, B, range(24), range(24))
+    bits_ref = ex.error_bits(ref, A, B, range(24), range(24))
+    assert bits[1] >= bits_ref[1] - 2.0, (bits, bits_ref)
+
+
+def test_fp64split_reference_compatible_mode(api, orc, inputs):
+    rng = np.random.default_rng(9)
+    A = inputs.reference_pd(rng, (16, 16), 4)
+    B = inputs.reference_pd(rng, (16, 16), 4)
+    C = host(api.gemm(dev(A), dev(B), "fp64split", split_exact=False))
+    ref = orc.gemm_fp64split(4, A, B, 16, 16, 16, exact=False)
+    assert np.allclose(C[..., 0], ref[..., 0], rtol=2.0 ** -50, atol=0)
+
+
+# --------------------------------------------------------- slice digits --
+
+@pytest.mark.parametrize("P,s", [(2, 14), (4, 28), (8, 55), (16, 108)])
+def test_digit_stages_bit_exact(api, orc, inputs, P, s):
+    rng = np.random.default_rng(s)
+    m, n, k = 20, 13, 37
+    A = inputs.uniform_pd(rng, (m, k), P)
+    B = inputs.uniform_pd(rng, (k, n), P)
+    A, _ = inputs.scale_rows(rng, A, -8, 8)
+    A[3] = 0.0
+    dA, dB = dev(A), dev(B)
+    E, F = api.scale_exponents(dA, dB)
+    Eo, Fo = orc.scale_exps(P, A, B, m, n, k)
+    assert np.array_equal(host(E), Eo) and np.array_equal(host(F), Fo)
+    pa = host(api.slice_digits(dA, E, s).float()).astype(np.int32)
+    pb = host(api.slice_digits(dB, F, s, trans=True).float()).astype(np.int32)
+    assert np.array_equal(pa, orc.digits(P, s, A, m, k, Eo, 0))
+    assert np.array_equal(pb, orc.digits(P, s, B, n, k, Fo, 1))
+    assert np.abs(pa).max() <= 128 and np.abs(pb).max() <= 128
+
+
+@pytest.mark.parametrize("engine", ["0", "1"])
+def test_diagonal_gemm_exact(api, orc, engine, monkeypatch):
+    monkeypatch.setenv("MDG_SLICE_ENGINE", engine)
+    rng = np.random.default_rng(int(engine) + 7)
+    s, D, m, n, k = 6, 9, 128, 256, 640
+    dA = rng.integers(-128, 129, size=(s, m, k)).astype(np.int32)
+    dB = rng.integers(-128, 129, size=(s, n, k)).astype(np.int32)
+    dA[:, :, :300] = 128  # the largest partial sums the flush interval allows
+    dB[:, :, :300] = -128
+    ref = orc.diag_sums(s, D, dA, dB, m, n, k)
+    got = host(api.slice_diagonals(dev(dA).to(torch.bfloat16), dev(dB).to(torch.bfloat16), D))
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("P,D", [(2, 14), (4, 28), (8, 55), (16, 108)])
+def test_renorm_bit_exact(api, orc, P, D):
+    rng = np.random.default_rng(P)
+    m, n = 9, 21
+    Cd = rng.integers(-(2 ** 40), 2 ** 40, size=(D, m, n)).astype(np.int64)
+    Cd[:, 0, 0] = 0
+    Cd[:, 1, 1] = 0
+    Cd[-1, 1, 1] = -5
+    E = rng.integers(-40, 40, size=m).astype(np.int32)
+    F = rng.integers(-40, 40, size=n).astype(np.int32)
+    got = host(api.renorm_diagonals(dev(Cd), dev(E), dev(F), P))
+    assert np.array_equal(got, orc.renorm_diags(P, D, Cd, E, F, m, n))
+
+
+@pytest.mark.parametrize("engine", ["0", "1"])
+@pytest.mark.parametrize("P", [2, 4, 8])
+@pytest.mark.parametrize("shape", [(1, 1, 1), (33, 31, 70), (130, 129, 65)])
+def test_slice_gemm_bit_exact_against_oracle(api, orc, inputs, engine, P, shape, monkeypatch):
+    monkeypatch.setenv("MDG_SLICE_ENGINE", engine)
+    m, n, k = shape
+    rng = np.random.default_rng(m + n + k + P)
+    A = inputs.uniform_pd(rng, (m, k), P)
+    B = inputs.uniform_pd(rng, (k, n), P)
+    s = api.default_slices(P)
+    got = host(api.gemm(dev(A), dev(B), "slice_bf16"))
+    assert np.array_equal(got, orc.gemm_slices(P, s, s, A, B, m, n, k))
+
+
+@pytest.mark.parametrize("name", ["dd64", "qd1024", "od2048_spread"])
+def test_slice_error_bits_not_worse_than_plain(api, orc, inputs, name):
+    import oracle.exact as ex
+    P, A, B = inputs.workload(name, 48, 48, 96)
+    Cs = host(api.gemm(dev(A), dev(B), "slice_bf16"))
+    Cp = host(api.gemm(dev(A), dev(B), "plain"))
+    rows, cols = range(0, 48, 3), range(0, 48, 5)
+    es = ex.error_bits(Cs, A, B, rows, cols)
+    ep = ex.error_bits(Cp, A, B, rows, cols)
+    print(name, "slice", es, "plain", ep)
+    assert es[1] >= ep[1] - 1.0
+
+
+def test_host_entry_matches_device_entry(api, inputs):
+    P, A, B = inputs.workload("qd1024", 50, 40, 30)
+    for form in ("plain", "slice_bf16", "fp64split"):
+        dC = host(api.gemm(dev(A), dev(B), form))
+        hC = api.gemm_host(A, B, form)
+        assert np.array_equal(dC, hC), form
+
+
+def test_strided_operands(api, orc, inputs):
+    """Leading dimensions larger than the logical sizes (views of a wider
+    buffer) through the C ABI."""
+    import ctypes
+    L = pkg("_lib").lib()
+    P, A, B = inputs.workload("dd64", 24, 20, 28)
+    lda, ldb, ldc = 40, 33, 29
+    Aw = np.zeros((24, lda, P)); Aw[:, :28] = A
+    Bw = np.zeros((28, ldb, P)); Bw[:, :20] = B
+    Cw = torch.zeros((24, ldc, P), dtype=torch.float64, device="cuda")
+    dA, dB = dev(Aw), dev(Bw)
+    ref = orc.gemm_plain(P, A, B, 24, 20, 28)
+    for form in (0, 1, 2):
+        need = L.mdg_gemm_workspace_size(form, P, 24, 20, 28, None)
+        ws = torch.empty(max(need, 1), dtype=torch.uint8, device="cuda")
+        Cw.zero_()
+        st = L.mdg_gemm(form, P, 24, 20, 28, ctypes.c_void_p(dA.data_ptr()), lda,
+                        ctypes.c_void_p(dB.data_ptr()), ldb, ctypes.c_void_p(Cw.data_ptr()), ldc,
+                        None, ctypes.c_void_p(ws.data_ptr()), need, None)
+        assert st == 0
+        torch.cuda.synchronize()
+        C = host(Cw)
+        assert np.all(C[:, 20:] == 0)
+        if form == 0:
+            assert np.array_equal(C[:, :20], ref)
+        else:
+            assert np.allclose(C[:, :20, 0], ref[..., 0], rtol=1e-15, atol=1e-15)
+
+
+def test_zero_k_gives_zero(api):
+    A = torch.zeros((5, 0, 4), dtype=torch.float64, device="cuda")
+    B = torch.zeros((0, 6, 4), dtype=torch.float64, device="cuda")
+    for form in ("plain", "fp64split", "slice_bf16"):
+        C = api.gemm(A, B, form, out=torch.full((5, 6, 4), 3.0, dtype=torch.float64,
+                                                 device="cuda"))
+        assert torch.all(C == 0)
