@@ -157,16 +157,34 @@ int mdg_slice_digits(int p, int s, int rows, int cols, const double *X,
                      int ldx, const int *E, int trans, void *planes,
                      int ld_out, long long plane_stride, void *stream);
 
-/* Exact diagonal sums Cd[d][r][c] = sum_{i+j=d} sum_k dA_i[r][k] dB_j[c][k]
- * (int64) for d < D, on BF16 tensor cores. */
+/* Number of int32 chunk planes mdg_slice_diagonals writes: the products
+ * of diagonal d (its digit pairs times k/64 steps of 64) are cut into runs
+ * of 1024 steps, so each chunk holds at most 65536 products of magnitude
+ * <= 2^14 and its sum is an exact int32 with |sum| <= 2^30. */
+int mdg_slice_chunk_count(int s, int D, int k);
+
+/* Exact diagonal sums on BF16 tensor cores: for d < D the sum over i+j=d
+ * and over k of dA_i[r][k] dB_j[c][k], written as chunk planes
+ * chunks[q][r][c] (int32, m x n each, chunk q of diagonal d after those of
+ * diagonals 0..d-1).  dA: s planes m x ld (plane_a apart), dB: s planes
+ * n x ld; m % 128 == 0, n % 256 == 0, k % 64 == 0. */
 int mdg_slice_diagonals(int s, int D, int m, int n, int k, const void *dA,
                         const void *dB, int ld, long long plane_a,
-                        long long plane_b, long long *Cd, void *stream);
+                        long long plane_b, int *chunks, void *stream);
 
-/* C[r][c] = RN_P( sum_d Cd[d][r][c] 256^(D-1-d) ) * 2^(E[r]+F[c]-14-8(D-1)). */
-int mdg_renorm_diagonals(int p, int D, int m, int n, const long long *Cd,
+/* C[r][c] = RN_P( sum_d C_d[r][c] 256^(D-1-d) ) * 2^(E[r]+F[c]-14-8(D-1)),
+ * C_d the sum of the chunks of diagonal d (layout of mdg_slice_diagonals
+ * for s digits and depth k; chunk planes are plane_c elements apart with
+ * row stride ldcd); each limb is rounded to nearest. */
+int mdg_renorm_diagonals(int p, int s, int D, int k, int m, int n,
+                         const int *chunks, long long plane_c, int ldcd,
                          const int *E, const int *F, double *C, int ldc,
                          void *stream);
+
+/* Waits for the device and reports MDG_ERROR_TIMEOUT when a bounded wait
+ * inside a tensor-core kernel gave up since the previous call (the record
+ * is then cleared); MDG_SUCCESS otherwise. */
+int mdg_device_status(void);
 
 #ifdef __cplusplus
 }

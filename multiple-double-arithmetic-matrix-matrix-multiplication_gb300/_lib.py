@@ -46,8 +46,11 @@ SIGNATURES = {
     "mdg_slice_conv": (c_int, [c_int] * 4 + [c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
     "mdg_scale_exponents": (c_int, [c_int] * 4 + [c_vp, c_int, c_vp, c_int, c_vp, c_vp, c_vp]),
     "mdg_slice_digits": (c_int, [c_int] * 4 + [c_vp, c_int, c_vp, c_int, c_vp, c_int, c_ll, c_vp]),
+    "mdg_slice_chunk_count": (c_int, [c_int] * 3),
     "mdg_slice_diagonals": (c_int, [c_int] * 5 + [c_vp, c_vp, c_int, c_ll, c_ll, c_vp, c_vp]),
-    "mdg_renorm_diagonals": (c_int, [c_int] * 4 + [c_vp, c_vp, c_vp, c_vp, c_int, c_vp]),
+    "mdg_renorm_diagonals": (c_int, [c_int] * 6 + [c_vp, c_ll, c_int, c_vp, c_vp, c_vp, c_int,
+                                                   c_vp]),
+    "mdg_device_status": (c_int, []),
 }
 
 _lib = None

@@ -191,19 +191,39 @@ def slice_digits(X, E, s, trans=False):
 
 
 def slice_diagonals(dA, dB, D):
-    """Exact diagonal sums of digit planes dA (s, m, k), dB (s, n, k); m, n
-    multiples of 128, k of 64."""
+    """Exact diagonal sums of digit planes dA (s, m, k), dB (s, n, k); m a
+    multiple of 128, n of 256, k of 64.  Returns the int32 chunk planes
+    (chunks, m, n) of the C ABI."""
     s, m, k = dA.shape
     n = dB.shape[1]
-    Cd = torch.empty((D, m, n), dtype=torch.int64, device=dA.device)
+    nch = lib().mdg_slice_chunk_count(s, D, k)
+    Cd = torch.empty((nch, m, n), dtype=torch.int32, device=dA.device)
     check(lib().mdg_slice_diagonals(s, D, m, n, k, _ptr(dA), _ptr(dB), k, m * k, n * k, _ptr(Cd),
                                     _stream(None)), "mdg_slice_diagonals")
     return Cd
 
 
-def renorm_diagonals(Cd, E, F, p):
-    D, m, n = Cd.shape
+def chunks_to_diagonals(Cd, s, D, k):
+    """Sum the chunk planes of each diagonal (int64), host side."""
+    KB = -(-max(k, 1) // 64)
+    out, q = [], 0
+    x = Cd.cpu().numpy().astype(np.int64)
+    for d in range(D):
+        lo, hi = max(0, d - (s - 1)), min(d, s - 1)
+        nc = -(-((hi - lo + 1) * KB) // 1024)
+        out.append(x[q:q + nc].sum(axis=0))
+        q += nc
+    return np.stack(out)
+
+
+def renorm_diagonals(Cd, E, F, p, s, D, k):
+    """Round chunk planes (chunks, m, n) to P-doubles (m, n, P)."""
+    _, m, n = Cd.shape
     C = torch.empty((m, n, p), dtype=torch.float64, device=Cd.device)
-    check(lib().mdg_renorm_diagonals(p, D, m, n, _ptr(Cd), _ptr(E), _ptr(F), _ptr(C), n,
-                                     _stream(None)), "mdg_renorm_diagonals")
+    check(lib().mdg_renorm_diagonals(p, s, D, k, m, n, _ptr(Cd), m * n, n, _ptr(E), _ptr(F),
+                                     _ptr(C), n, _stream(None)), "mdg_renorm_diagonals")
     return C
+
+
+def device_status():
+    return lib().mdg_device_status()

@@ -22,7 +22,7 @@ void set_cuda_error(cudaError_t e) {
 int default_engine() {
   const char *v = std::getenv("MDG_SLICE_ENGINE");
   if (v && *v) return std::atoi(v) ? 1 : 0;
-  return 1;
+  return 0;
 }
 
 // ------------------------------------------------------------------ cache --
@@ -382,28 +382,40 @@ int mdg_slice_digits(int p, int s, int rows, int cols, const double *X, int ldx,
                        cols, as_stream(stream));
 }
 
+int mdg_slice_chunk_count(int s, int D, int k) {
+  if (s < 1 || D < 1 || D > 2 * s - 1 || k < 0) return 0;
+  return total_chunks(s, D, (int)(align_up(std::max(k, 1), 64) / 64));
+}
+
 int mdg_slice_diagonals(int s, int D, int m, int n, int k, const void *dA, const void *dB, int ld,
-                        long long plane_a, long long plane_b, long long *Cd, void *stream) {
+                        long long plane_a, long long plane_b, int *chunks, void *stream) {
   if (s < 1 || D < 1 || D > 2 * s - 1 || m < 0 || n < 0 || k < 0) return MDG_ERROR_INVALID_SIZE;
-  if (m % 128 || n % 128 || k % 64 || ld < k) return MDG_ERROR_INVALID_SIZE;
-  if (m == 0 || n == 0) return MDG_SUCCESS;
-  if (!dA || !dB || !Cd) return MDG_ERROR_NULL_POINTER;
+  if (m % 128 || n % 256 || k % 64 || ld < k) return MDG_ERROR_INVALID_SIZE;
+  if (m == 0 || n == 0 || k == 0) return MDG_SUCCESS;
+  if (!dA || !dB || !chunks) return MDG_ERROR_NULL_POINTER;
   const long long plane_c = (long long)m * n;
-  if (default_engine() == 1)
-    return launch_diag_gemm_tc(s, D, m, n, k, dA, dB, ld, plane_a, plane_b, Cd, plane_c, n,
+  if (default_engine() == 1 && ld == k)
+    return launch_diag_gemm_tc(s, D, m, n, k, dA, dB, ld, plane_a, plane_b, chunks, plane_c,
                                as_stream(stream));
-  return launch_diag_gemm_v0(s, D, m, n, k, dA, dB, ld, plane_a, plane_b, Cd, plane_c, n,
+  return launch_diag_gemm_v0(s, D, m, n, k, dA, dB, ld, plane_a, plane_b, chunks, plane_c,
                              as_stream(stream));
 }
 
-int mdg_renorm_diagonals(int p, int D, int m, int n, const long long *Cd, const int *E,
-                         const int *F, double *C, int ldc, void *stream) {
+int mdg_renorm_diagonals(int p, int s, int D, int k, int m, int n, const int *chunks,
+                         long long plane_c, int ldcd, const int *E, const int *F, double *C,
+                         int ldc, void *stream) {
   if (!valid_p(p)) return MDG_ERROR_INVALID_LIMBS;
-  if (D < 1 || m < 0 || n < 0 || ldc < std::max(n, 1)) return MDG_ERROR_INVALID_SIZE;
+  if (s < 1 || D < 1 || D > 2 * s - 1 || k < 0 || m < 0 || n < 0 || ldc < std::max(n, 1) ||
+      ldcd < n || plane_c < (long long)m * ldcd)
+    return MDG_ERROR_INVALID_SIZE;
+  if (!words_for(1, D)) return MDG_ERROR_NOT_SUPPORTED;
   if (m == 0 || n == 0) return MDG_SUCCESS;
-  if (!Cd || !E || !F || !C) return MDG_ERROR_NULL_POINTER;
+  if (!chunks || !E || !F || !C) return MDG_ERROR_NULL_POINTER;
   if (m > 65535) return MDG_ERROR_NOT_SUPPORTED;
-  return launch_renorm(p, D, m, n, Cd, (long long)m * n, n, E, F, C, ldc, as_stream(stream));
+  const int KB = (int)(align_up(std::max(k, 1), 64) / 64);
+  return launch_renorm(p, s, D, KB, m, n, chunks, plane_c, ldcd, E, F, C, ldc, as_stream(stream));
 }
+
+int mdg_device_status(void) { return tc_device_status(); }
 
 }  // extern "C"

@@ -1,10 +1,414 @@
-// placeholder, replaced by the tcgen05 engine
+// Diagonal GEMM of digit planes on the 5th-generation tensor cores.
+//
+// For every output tile (128 rows x 256 columns) and every diagonal d < D,
+// the products A_i B_j^T with i + j = d are summed over k exactly: BF16
+// digits in [-128, 128], FP32 accumulation in tensor memory (TMEM), flushed
+// every 256 products (|partial| <= 2^22) into int32 registers, stored every
+// 65536 products as one int32 chunk plane (|sum| <= 2^30).
+//
+// One CTA per SM, persistent over tiles; 10 warps with fixed roles:
+//   warp 0      TMA producer: A_i (128 x 64) and B_j (256 x 64) k-blocks
+//               into a 4-stage shared-memory ring (128-byte swizzle),
+//   warp 1      TMEM allocator and MMA issuer: tcgen05.mma kind::f16,
+//               M=128 N=256 K=16, BF16 x BF16 -> FP32, into one of two
+//               256-column accumulators (all 512 TMEM columns),
+//   warps 2-9   epilogue: tcgen05.ld of the accumulator (warp w reads TMEM
+//               lanes 32 (w % 4) .. +31, columns 128 ((w - 2) / 4) .. +127),
+//               exact float -> int conversion, int32 accumulation, chunk
+//               stores.
+// Barriers: full/empty per stage (TMA <-> MMA), accfull/accempty per
+// accumulator (MMA <-> epilogue).  Every wait is bounded (2 s of
+// %globaltimer); on a timeout the CTA records the error, stops issuing,
+// waits (bounded) for its copies and MMAs in flight, frees TMEM and exits.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "common.cuh"
 #include "slice_tc.cuh"
+
+namespace {
+
+constexpr int TM = 128, TN = 256, TK = 64;
+constexpr int STAGES = 4;
+constexpr int A_BYTES = TM * TK * 2;  // 16 KiB
+constexpr int B_BYTES = TN * TK * 2;  // 32 KiB
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int EPI_WARPS = 8;
+constexpr int THREADS = 32 * (2 + EPI_WARPS);
+constexpr int TMEM_COLS = 512;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /* align */ + 256 /* barriers */;
+constexpr unsigned long long TIMEOUT_NS = 2000000000ull;
+
+// kind::f16 instruction descriptor: D F32 (bits 4-5 = 1), A BF16 (7-9 = 1),
+// B BF16 (10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit 17,
+// M >> 4 at bit 24.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
+                           ((uint32_t)(TM >> 4) << 24);
+
+__device__ int g_tc_error = 0;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait.  Returns false on a timeout (and raises the CTA's abort
+// flag) or when another role has already aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort) {
+  if (mbar_test(bar, parity)) return true;
+  const unsigned long long t0 = now_ns();
+  while (true) {
+    if (mbar_test(bar, parity)) return true;
+    if (*abort) return false;
+    if (now_ns() - t0 > TIMEOUT_NS) {
+      *abort = 1;
+      return false;
+    }
+  }
+}
+
+// Bounded wait that ignores the abort flag (draining in-flight work).
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+  const unsigned long long t0 = now_ns();
+  while (!mbar_test(bar, parity) && now_ns() - t0 < TIMEOUT_NS) {
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *tm, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor, K-major, 128-byte swizzle: start address
+// >> 4 (bits 0-13), leading byte offset 16 B (unused for this layout,
+// bits 16-29), stride byte offset 1024 B between 8-row groups (bits 32-45),
+// descriptor version 1 (bits 46-47), swizzle mode 2 = 128 B (bits 61-63).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(16 >> 4) << 16) |
+         ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(IDESC), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    diag_gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA,
+                        const __grid_constant__ CUtensorMap tmB, int s, int D, int Mp, int Np,
+                        int KB, int *__restrict__ out, long long plane_c) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES);
+  // bars: [0,4) full, [4,8) empty, [8,10) accfull, [10,12) accempty, 12 mma drain
+  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bars + 16);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 17);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t smem_base = smem_u32(smem);
+  auto full = [&](int st) { return smem_u32(bars + st); };
+  auto empty = [&](int st) { return smem_u32(bars + STAGES + st); };
+  auto accfull = [&](int b) { return smem_u32(bars + 2 * STAGES + b); };
+  auto accempty = [&](int b) { return smem_u32(bars + 2 * STAGES + 2 + b); };
+  const uint32_t drain_bar = smem_u32(bars + 2 * STAGES + 4);
+
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < STAGES; ++st) {
+      mbar_init(full(st), 1);
+      mbar_init(empty(st), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accfull(b), 1);
+      mbar_init(accempty(b), EPI_WARPS);
+    }
+    mbar_init(drain_bar, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_holder)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem_base = *tmem_holder;
+
+  const int MB = Mp / TM;
+  const int tiles = MB * (Np / TN);
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ------------------------------------------------------ producer --
+      int st = 0;
+      uint32_t ph = 0;
+      uint32_t last_par[STAGES];
+      bool issued[STAGES];
+      for (int i = 0; i < STAGES; ++i) issued[i] = false;
+      for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int row = (tile % MB) * TM, col = (tile / MB) * TN;
+        for (int d = 0; d < D; ++d) {
+          const int ilo = d - (s - 1) > 0 ? d - (s - 1) : 0;
+          const int S = mdgi::diag_pairs(d, s) * KB;
+          for (int t = 0; t < S; ++t) {
+            const int i = ilo + t / KB, kb = t - (t / KB) * KB, j = d - i;
+            if (!mbar_wait(empty(st), ph ^ 1, abort_flag)) goto producer_done;
+            mbar_expect_tx(full(st), STAGE_BYTES);
+            const uint32_t a_dst = smem_base + st * STAGE_BYTES;
+            tma_load_2d(a_dst, &tmA, kb * TK, i * Mp + row, full(st));
+            tma_load_2d(a_dst + A_BYTES, &tmB, kb * TK, j * Np + col, full(st));
+            last_par[st] = ph;
+            issued[st] = true;
+            if (++st == STAGES) {
+              st = 0;
+              ph ^= 1;
+            }
+          }
+        }
+      }
+    producer_done:
+      if (*abort_flag)
+        for (int i = 0; i < STAGES; ++i)
+          if (issued[i]) mbar_drain(full(i), last_par[i]);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------------------------------------------- MMA issuer --
+      int st = 0, buf = 0;
+      uint32_t ph = 0, aph[2] = {0, 0};
+      bool any = false;
+      for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        for (int d = 0; d < D; ++d) {
+          const int S = mdgi::diag_pairs(d, s) * KB;
+          for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
+            if (!mbar_wait(accempty(buf), aph[buf] ^ 1, abort_flag)) goto mma_done;
+            fence_after();
+            const uint32_t dt = tmem_base + buf * TN;
+            const int g1 = g0 + mdgi::GROUP_STEPS < S ? g0 + mdgi::GROUP_STEPS : S;
+            for (int t = g0; t < g1; ++t) {
+              if (!mbar_wait(full(st), ph, abort_flag)) goto mma_done;
+              fence_after();
+              const uint32_t a_addr = smem_base + st * STAGE_BYTES;
+              const uint64_t da = sw128_desc(a_addr), db = sw128_desc(a_addr + A_BYTES);
+#pragma unroll
+              for (int kk = 0; kk < TK / 16; ++kk)
+                mma_bf16(dt, da + 2 * kk, db + 2 * kk, (t > g0 || kk > 0) ? 1u : 0u);
+              mma_commit(empty(st));
+              any = true;
+              if (++st == STAGES) {
+                st = 0;
+                ph ^= 1;
+              }
+            }
+            mma_commit(accfull(buf));
+            aph[buf] ^= 1;
+            buf ^= 1;
+          }
+        }
+      }
+    mma_done:
+      if (*abort_flag && any) {
+        mma_commit(drain_bar);
+        mbar_drain(drain_bar, 0);
+      }
+    }
+  } else {
+    // -------------------------------------------------------- epilogue --
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    int acc[128];
+#pragma unroll
+    for (int j = 0; j < 128; ++j) acc[j] = 0;
+    int buf = 0;
+    uint32_t aph[2] = {0, 0};
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+      const int row = (tile % MB) * TM + 32 * q + lane;
+      const int col = (tile / MB) * TN + 128 * h;
+      int chunk = 0;
+      for (int d = 0; d < D; ++d) {
+        const int S = mdgi::diag_pairs(d, s) * KB;
+        for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
+          // lane 0 waits; the verdict is broadcast so the warp stays
+          // converged for the .sync.aligned TMEM loads
+          int ok = 1;
+          if (lane == 0) ok = mbar_wait(accfull(buf), aph[buf], abort_flag) ? 1 : 0;
+          ok = __shfl_sync(0xffffffffu, ok, 0);
+          if (!ok) goto epi_done;
+          aph[buf] ^= 1;
+          fence_after();
+          const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + buf * TN + 128 * h;
+#pragma unroll
+          for (int c4 = 0; c4 < 4; ++c4) {
+            uint32_t r[32];
+            tmem_ld32(taddr + 32 * c4, r);
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              acc[32 * c4 + j] += __float_as_int(__uint_as_float(r[j]) + 12582912.0f) - 0x4B400000;
+          }
+          fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(accempty(buf));
+          buf ^= 1;
+          const int g1 = g0 + mdgi::GROUP_STEPS;
+          if (g1 % mdgi::CHUNK_STEPS == 0 || g1 >= S) {
+            int4 *dst = reinterpret_cast<int4 *>(out + (size_t)chunk * plane_c +
+                                                 (size_t)row * Np + col);
+#pragma unroll
+            for (int v = 0; v < 32; ++v) {
+              dst[v] = make_int4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
+              acc[4 * v] = acc[4 * v + 1] = acc[4 * v + 2] = acc[4 * v + 3] = 0;
+            }
+            ++chunk;
+          }
+        }
+      }
+    }
+  epi_done:;
+  }
+  __syncwarp();
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                 "r"(TMEM_COLS)
+                 : "memory");
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(&g_tc_error, 1);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 2-D map over `planes` planes of rows x Kp BF16 (row stride Kp), box
+// 64 x box_rows, 128-byte swizzle.
+int make_map(CUtensorMap *m, const void *base, int Kp, long long rows_total, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return MDG_ERROR_NOT_SUPPORTED;
+  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows_total};
+  cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
+  cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? MDG_SUCCESS : MDG_ERROR_NOT_SUPPORTED;
+}
+
+}  // namespace
+
 namespace mdgi {
+
 int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, const void *dB,
-                        int ld, long long plane_a, long long plane_b, long long *Cd,
-                        long long plane_c, int ldc, cudaStream_t st) {
-  return launch_diag_gemm_v0(s, D, Mp, Np, Kp, dA, dB, ld, plane_a, plane_b, Cd, plane_c, ldc, st);
+                        int ld, long long plane_a, long long plane_b, int *chunks,
+                        long long plane_c, cudaStream_t st) {
+  if (Mp % TM || Np % TN || Kp % TK || ld != Kp) return MDG_ERROR_INVALID_SIZE;
+  if (plane_a != (long long)Mp * Kp || plane_b != (long long)Np * Kp) return MDG_ERROR_INVALID_SIZE;
+  if ((reinterpret_cast<uintptr_t>(dA) | reinterpret_cast<uintptr_t>(dB)) & 15)
+    return MDG_ERROR_INVALID_SIZE;
+  CUtensorMap ma, mb;
+  MDG_TRY(make_map(&ma, dA, Kp, (long long)s * Mp, TM));
+  MDG_TRY(make_map(&mb, dB, Kp, (long long)s * Np, TN));
+  static int configured_dev = -1;
+  int dev = 0, sms = 0;
+  MDG_TRY_CUDA(cudaGetDevice(&dev));
+  if (configured_dev != dev) {
+    MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    configured_dev = dev;
+  }
+  MDG_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int tiles = (Mp / TM) * (Np / TN);
+  const int grid = tiles < sms ? tiles : sms;
+  diag_gemm_tc_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(ma, mb, s, D, Mp, Np, Kp / TK, chunks,
+                                                         plane_c);
+  MDG_TRY_LAUNCH();
+  return MDG_SUCCESS;
 }
+
+int tc_device_status() {
+  MDG_TRY_CUDA(cudaDeviceSynchronize());
+  int flag = 0, zero = 0;
+  MDG_TRY_CUDA(cudaMemcpyFromSymbol(&flag, g_tc_error, sizeof(int)));
+  if (flag) {
+    MDG_TRY_CUDA(cudaMemcpyToSymbol(g_tc_error, &zero, sizeof(int)));
+    return MDG_ERROR_TIMEOUT;
+  }
+  return MDG_SUCCESS;
 }
+
+}  // namespace mdgi

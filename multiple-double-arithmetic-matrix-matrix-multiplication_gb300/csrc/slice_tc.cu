@@ -12,8 +12,11 @@
 // 3. diagonal GEMM.  C_d = sum_{i+j=d} A_i B_j^T for d < D.  One product
 //    of two digits is at most 2^14, so an FP32 accumulator holds the exact
 //    sum of 256 of them (|sum| <= 2^22); every 256 products the FP32
-//    accumulator is flushed into 64-bit integers.  All sums are exact.
-// 4. renormalisation.  W = sum_d C_d 256^(D-1-d) is formed exactly in
+//    accumulator is flushed into 32-bit integers, and every 65536 products
+//    the integers are stored as one "chunk" plane (|sum| <= 2^30).  All
+//    sums are exact.
+// 4. renormalisation.  W = sum_d C_d 256^(D-1-d), C_d the sum of the
+//    chunks of diagonal d, is formed exactly in
 //    wide integers and rounded to P limbs, each to nearest, scaled by
 //    2^(E[r] + F[c] - 14 - 8 (D - 1)).
 // The reference has no counterpart of steps 1-4; its split form cuts limbs
@@ -147,17 +150,19 @@ __device__ __forceinline__ int64_t exact_int(float x) {
 __global__ void __launch_bounds__(256)
     diag_gemm_v0(int s, int D, int Kp, const __nv_bfloat16 *__restrict__ dA,
                  const __nv_bfloat16 *__restrict__ dB, int ld, long long plane_a,
-                 long long plane_b, long long *__restrict__ Cd, long long plane_c, int ldc) {
+                 long long plane_b, int *__restrict__ out, long long plane_c, int ldc) {
   __shared__ __align__(16) __nv_bfloat16 As[BM][SK];
   __shared__ __align__(16) __nv_bfloat16 Bs[BN][SK];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int g = lane >> 2, t = lane & 3;
   const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
   const int row0 = blockIdx.y * BM, col0 = blockIdx.x * BN;
+  const int KB = Kp / 64;
+  int chunk = 0;
 
   for (int d = 0; d < D; ++d) {
     float acc[2][4][4];
-    int64_t tot[2][4][4];
+    int tot[2][4][4];
 #pragma unroll
     for (int a = 0; a < 2; ++a)
 #pragma unroll
@@ -167,23 +172,23 @@ __global__ void __launch_bounds__(256)
           acc[a][b][c] = 0.f;
           tot[a][b][c] = 0;
         }
-    int terms = 0;
-    const int ilo = max(0, d - (s - 1)), ihi = min(d, s - 1);
-    for (int i = ilo; i <= ihi; ++i) {
-      const __nv_bfloat16 *Ai = dA + i * plane_a + (size_t)row0 * ld;
-      const __nv_bfloat16 *Bj = dB + (d - i) * plane_b + (size_t)col0 * ld;
-      for (int k0 = 0; k0 < Kp; k0 += BK) {
-        // A: 128 x 32 = 512 vectors of 8; B: 64 x 32 = 256 vectors
+    const int ilo = max(0, d - (s - 1));
+    const int S = mdgi::diag_pairs(d, s) * KB;
+    for (int step = 0; step < S; ++step) {
+      const int i = ilo + step / KB, kb = step % KB;
+      const __nv_bfloat16 *Ai = dA + i * plane_a + (size_t)row0 * ld + kb * 64;
+      const __nv_bfloat16 *Bj = dB + (d - i) * plane_b + (size_t)col0 * ld + kb * 64;
+      for (int half = 0; half < 2; ++half) {
 #pragma unroll
         for (int v = tid; v < BM * BK / 8; v += 256) {
           const int r = v >> 2, cc = (v & 3) * 8;
           *reinterpret_cast<uint4 *>(&As[r][cc]) =
-              *reinterpret_cast<const uint4 *>(Ai + (size_t)r * ld + k0 + cc);
+              *reinterpret_cast<const uint4 *>(Ai + (size_t)r * ld + half * BK + cc);
         }
         {
           const int r = tid >> 2, cc = (tid & 3) * 8;
           *reinterpret_cast<uint4 *>(&Bs[r][cc]) =
-              *reinterpret_cast<const uint4 *>(Bj + (size_t)r * ld + k0 + cc);
+              *reinterpret_cast<const uint4 *>(Bj + (size_t)r * ld + half * BK + cc);
         }
         __syncthreads();
 #pragma unroll
@@ -209,40 +214,43 @@ __global__ void __launch_bounds__(256)
             for (int nt = 0; nt < 4; ++nt) mma_bf16(acc[mt][nt], af[mt], bf[nt]);
         }
         __syncthreads();
-        terms += BK;
-        if (terms == 256) {
+      }
+      const bool group_end = (step % mdgi::GROUP_STEPS == mdgi::GROUP_STEPS - 1) || step == S - 1;
+      const bool chunk_end = (step % mdgi::CHUNK_STEPS == mdgi::CHUNK_STEPS - 1) || step == S - 1;
+      if (group_end) {
 #pragma unroll
-          for (int a = 0; a < 2; ++a)
+        for (int a = 0; a < 2; ++a)
 #pragma unroll
-            for (int b = 0; b < 4; ++b)
+          for (int b = 0; b < 4; ++b)
 #pragma unroll
-              for (int c = 0; c < 4; ++c) {
-                tot[a][b][c] += exact_int(acc[a][b][c]);
-                acc[a][b][c] = 0.f;
-              }
-          terms = 0;
-        }
+            for (int c = 0; c < 4; ++c) {
+              tot[a][b][c] += (int)exact_int(acc[a][b][c]);
+              acc[a][b][c] = 0.f;
+            }
+      }
+      if (chunk_end) {
+        int *o = out + (size_t)chunk * plane_c;
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+          for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const int r = row0 + wm + mt * 16 + g + h * 8;
+              const int c = col0 + wn + nt * 8 + 2 * t;
+              *reinterpret_cast<int2 *>(o + (size_t)r * ldc + c) =
+                  make_int2(tot[mt][nt][2 * h], tot[mt][nt][2 * h + 1]);
+              tot[mt][nt][2 * h] = tot[mt][nt][2 * h + 1] = 0;
+            }
+        ++chunk;
       }
     }
-    long long *out = Cd + d * plane_c;
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-      for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int r = row0 + wm + mt * 16 + g + h * 8;
-          const int c = col0 + wn + nt * 8 + 2 * t;
-          const long long v0 = tot[mt][nt][2 * h] + exact_int(acc[mt][nt][2 * h]);
-          const long long v1 = tot[mt][nt][2 * h + 1] + exact_int(acc[mt][nt][2 * h + 1]);
-          *reinterpret_cast<longlong2 *>(out + (size_t)r * ldc + c) = make_longlong2(v0, v1);
-        }
   }
 }
 
 // --------------------------------------------------------------- renorm --
 template <int P, int NW>
-__global__ void renorm_kernel(int D, int m, int n, const long long *__restrict__ Cd,
+__global__ void renorm_kernel(int s, int D, int KB, int m, int n, const int *__restrict__ chunks,
                               long long plane_c, int ldcd, const int *__restrict__ E,
                               const int *__restrict__ F, double *__restrict__ C, int ldc) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -251,9 +259,12 @@ __global__ void renorm_kernel(int D, int m, int n, const long long *__restrict__
   uint64_t w[NW];
 #pragma unroll
   for (int i = 0; i < NW; ++i) w[i] = 0;
-  const long long *src = Cd + (size_t)r * ldcd + c;
+  const int *src = chunks + (size_t)r * ldcd + c;
+  int q = 0;
   for (int d = 0; d < D; ++d) {
-    const long long v = src[d * plane_c];
+    long long v = 0;
+    const int nc = mdgi::diag_chunks(d, s, KB);
+    for (int j = 0; j < nc; ++j, ++q) v += src[q * plane_c];
     if (v) wide_add_shifted<NW>(w, v, 8 * (D - 1 - d));
   }
   const int scale = E[r] + F[c] - 14 - 8 * (D - 1);
@@ -307,8 +318,9 @@ SlicePlan make_slice_plan(int p, int s, int D, int m, int n, int k) {
   pl.n = n;
   pl.k = k;
   pl.Mp = (int)align_up(std::max(m, 1), 128);
-  pl.Np = (int)align_up(std::max(n, 1), 128);
+  pl.Np = (int)align_up(std::max(n, 1), 256);
   pl.Kp = (int)align_up(std::max(k, 1), 64);
+  pl.chunks = total_chunks(s, D, pl.Kp / 64);
   size_t off = 0;
   auto take = [&](size_t bytes) {
     const size_t o = off;
@@ -324,7 +336,7 @@ SlicePlan make_slice_plan(int p, int s, int D, int m, int n, int k) {
   pl.plane_c = (long long)pl.Mp * pl.Np;
   pl.off_dA = take(sizeof(__nv_bfloat16) * (size_t)s * pl.plane_a);
   pl.off_dB = take(sizeof(__nv_bfloat16) * (size_t)s * pl.plane_b);
-  pl.off_Cd = take(sizeof(long long) * (size_t)D * pl.plane_c);
+  pl.off_Cd = take(sizeof(int) * (size_t)pl.chunks * pl.plane_c);
   pl.total = off;
   return pl;
 }
@@ -378,25 +390,26 @@ int launch_digits(int p, int s, int rows, int cols, const double *X, int ldx, co
 }
 
 int launch_diag_gemm_v0(int s, int D, int Mp, int Np, int Kp, const void *dA, const void *dB,
-                        int ld, long long plane_a, long long plane_b, long long *Cd,
-                        long long plane_c, int ldc, cudaStream_t st) {
-  if (Mp % BM || Np % BN || Kp % BK) return MDG_ERROR_INVALID_SIZE;
+                        int ld, long long plane_a, long long plane_b, int *chunks,
+                        long long plane_c, cudaStream_t st) {
+  if (Mp % BM || Np % BN || Kp % 64) return MDG_ERROR_INVALID_SIZE;
   dim3 grid(Np / BN, Mp / BM);
   diag_gemm_v0<<<grid, 256, 0, st>>>(s, D, Kp, reinterpret_cast<const __nv_bfloat16 *>(dA),
                                      reinterpret_cast<const __nv_bfloat16 *>(dB), ld, plane_a,
-                                     plane_b, Cd, plane_c, ldc);
+                                     plane_b, chunks, plane_c, Np);
   MDG_TRY_LAUNCH();
   return MDG_SUCCESS;
 }
 
-int launch_renorm(int p, int D, int m, int n, const long long *Cd, long long plane_c, int ldcd,
-                  const int *E, const int *F, double *C, int ldc, cudaStream_t st) {
+int launch_renorm(int p, int s, int D, int KB, int m, int n, const int *chunks,
+                  long long plane_c, int ldcd, const int *E, const int *F, double *C, int ldc,
+                  cudaStream_t st) {
   if (m == 0 || n == 0) return MDG_SUCCESS;
   const int NW = words_for(1, D);
   if (!NW) return MDG_ERROR_NOT_SUPPORTED;
   dim3 grid(ceil_div(n, 128), m);
 #define MDG_RENORM(PP, W)                                                                  \
-  renorm_kernel<PP, W><<<grid, 128, 0, st>>>(D, m, n, Cd, plane_c, ldcd, E, F, C, ldc)
+  renorm_kernel<PP, W><<<grid, 128, 0, st>>>(s, D, KB, m, n, chunks, plane_c, ldcd, E, F, C, ldc)
 #define MDG_RENORM_P(PP)           \
   switch (NW) {                    \
     case 4: MDG_RENORM(PP, 4); break;  \
@@ -426,7 +439,7 @@ int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *
   int *F = reinterpret_cast<int *>(base + pl.off_F);
   void *dA = base + pl.off_dA;
   void *dB = base + pl.off_dB;
-  auto *Cd = reinterpret_cast<long long *>(base + pl.off_Cd);
+  auto *Cd = reinterpret_cast<int *>(base + pl.off_Cd);
   MDG_TRY(launch_scale_exponents(pl.p, pl.m, pl.n, pl.k, A, lda, B, ldb, rowbits, colbits, E, F,
                                  st));
   MDG_TRY(launch_digits(pl.p, pl.s, pl.m, pl.k, A, lda, E, 0, dA, pl.Kp, pl.plane_a, pl.Mp,
@@ -435,12 +448,13 @@ int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *
                         pl.Kp, st));
   if (engine == 1) {
     MDG_TRY(launch_diag_gemm_tc(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
-                                pl.plane_b, Cd, pl.plane_c, pl.Np, st));
+                                pl.plane_b, Cd, pl.plane_c, st));
   } else {
     MDG_TRY(launch_diag_gemm_v0(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
-                                pl.plane_b, Cd, pl.plane_c, pl.Np, st));
+                                pl.plane_b, Cd, pl.plane_c, st));
   }
-  MDG_TRY(launch_renorm(pl.p, pl.D, pl.m, pl.n, Cd, pl.plane_c, pl.Np, E, F, C, ldc, st));
+  MDG_TRY(launch_renorm(pl.p, pl.s, pl.D, pl.Kp / 64, pl.m, pl.n, Cd, pl.plane_c, pl.Np, E, F,
+                        C, ldc, st));
   return MDG_SUCCESS;
 }
 

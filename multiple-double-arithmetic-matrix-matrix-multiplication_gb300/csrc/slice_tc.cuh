@@ -6,11 +6,33 @@
 
 namespace mdgi {
 
+// The diagonal sums are written as int32 "chunk" planes: the products of
+// diagonal d (pairs_d digit pairs times Kp/64 k-steps of 64) are cut into
+// runs of CHUNK_STEPS k-steps, at most 65536 products of |d_i d_j| <= 2^14,
+// so every chunk sum is an exact int32 with |sum| <= 2^30.  Chunks are
+// numbered diagonal by diagonal.
+constexpr int CHUNK_STEPS = 1024;
+constexpr int GROUP_STEPS = 4;  // k-steps per FP32 flush: 256 products, |sum| <= 2^22
+
+__host__ __device__ inline int diag_pairs(int d, int s) {
+  const int lo = d - (s - 1) > 0 ? d - (s - 1) : 0, hi = d < s - 1 ? d : s - 1;
+  return hi - lo + 1;
+}
+__host__ __device__ inline int diag_chunks(int d, int s, int KB) {
+  return (diag_pairs(d, s) * KB + CHUNK_STEPS - 1) / CHUNK_STEPS;
+}
+inline int total_chunks(int s, int D, int KB) {
+  int c = 0;
+  for (int d = 0; d < D; ++d) c += diag_chunks(d, s, KB);
+  return c;
+}
+
 // Workspace layout of one slice-digit GEMM (byte offsets, 256-aligned).
 struct SlicePlan {
   int p, s, D, m, n, k;
-  int Mp, Np, Kp;  // padded to 128, 128, 64
-  long long plane_a, plane_b, plane_c;  // elements between digit / diagonal planes
+  int Mp, Np, Kp;  // padded to 128, 256, 64
+  int chunks;
+  long long plane_a, plane_b, plane_c;  // elements between digit / chunk planes
   size_t off_rowbits, off_colbits, off_E, off_F, off_dA, off_dB, off_Cd, total;
 };
 
@@ -23,16 +45,21 @@ int launch_scale_exponents(int p, int m, int n, int k, const double *A, int lda,
 int launch_digits(int p, int s, int rows, int cols, const double *X, int ldx, const int *E,
                   int trans, void *planes, int ld_out, long long plane_stride, int rows_pad,
                   int cols_pad, cudaStream_t st);
-// mma.sync engine (Mp % 128, Np % 64, Kp % 32)
+// Engines write chunk planes of Mp x Np int32 (row stride Np).
+// mma.sync engine (Mp % 128, Np % 64, Kp % 64)
 int launch_diag_gemm_v0(int s, int D, int Mp, int Np, int Kp, const void *dA, const void *dB,
-                        int ld, long long plane_a, long long plane_b, long long *Cd,
-                        long long plane_c, int ldc, cudaStream_t st);
-// tcgen05 engine (Mp % 128, Np % 128, Kp % 64)
+                        int ld, long long plane_a, long long plane_b, int *chunks,
+                        long long plane_c, cudaStream_t st);
+// tcgen05 engine (Mp % 128, Np % 256, Kp % 64, ld == Kp)
 int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, const void *dB,
-                        int ld, long long plane_a, long long plane_b, long long *Cd,
-                        long long plane_c, int ldc, cudaStream_t st);
-int launch_renorm(int p, int D, int m, int n, const long long *Cd, long long plane_c, int ldcd,
-                  const int *E, const int *F, double *C, int ldc, cudaStream_t st);
+                        int ld, long long plane_a, long long plane_b, int *chunks,
+                        long long plane_c, cudaStream_t st);
+int launch_renorm(int p, int s, int D, int KB, int m, int n, const int *chunks,
+                  long long plane_c, int ldcd, const int *E, const int *F, double *C, int ldc,
+                  cudaStream_t st);
+// Waits for the device; MDG_ERROR_TIMEOUT if a bounded wait of the tcgen05
+// engine gave up since the last call (the flag is then cleared).
+int tc_device_status();
 
 // engine: 0 = mma.sync, 1 = tcgen05
 int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *B, int ldb,

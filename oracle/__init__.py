@@ -154,7 +154,7 @@ def digits(P, s, x, rows, cols, E, trans):
 def diag_sums(s, D, dA, dB, m, n, k):
     dA = np.ascontiguousarray(dA, dtype=np.int32)
     dB = np.ascontiguousarray(dB, dtype=np.int32)
-    Cd = np.zeros((D + 1, m, n), dtype=np.int64)
+    Cd = np.zeros((D, m, n), dtype=np.int64)
     lib().orc_diag_sums(s, D, m, n, k, _ptr(dA, _ip), _ptr(dB, _ip), _ptr(Cd, _lp))
     return Cd
 

@@ -611,9 +611,9 @@ void orc_plane_conv(int n, int pp, const double *A, const double *B,
  * and V as s balanced base-256 digits d_0 (most significant) .. d_{s-1},
  * each in [-128, 128].  The product of two digit planes is exact in BF16
  * with FP32 accumulation; the sums C_d = sum_{i+j=d} A_i B_j over the
- * diagonals d <= D are exact integers; the result is
- * W = sum_d C_d 256^(D-d) scaled by 2^(E + F - 14 - 8 D), rounded to P
- * limbs, each to nearest. */
+ * D diagonals d < D are exact integers; the result is
+ * W = sum_d C_d 256^(D-1-d) scaled by 2^(E + F - 14 - 8 (D-1)), rounded to
+ * P limbs, each to nearest. */
 
 #define NW 16 /* 64-bit words of the fixed-point integers: 1024 bits */
 
@@ -783,12 +783,12 @@ void orc_digits(int P, int s, int rows, int cols, const double *x,
 }
 
 /* Exact diagonal sums C_d[r][c] = sum_{i+j=d} sum_kk dA_i[r][kk] dB_j[c][kk]
- * for d <= D (int64).  dA: s planes m x k;  dB: s planes n x k. */
+ * for d < D (int64).  dA: s planes m x k;  dB: s planes n x k. */
 void orc_diag_sums(int s, int D, int m, int n, int k, const int *dA,
                    const int *dB, int64_t *Cd) {
   long pa = (long)m * k, pb = (long)n * k, pc = (long)m * n;
   int d, i, r, c, kk;
-  for (d = 0; d <= D; ++d)
+  for (d = 0; d < D; ++d)
     for (r = 0; r < m; ++r)
       for (c = 0; c < n; ++c) {
         int64_t acc = 0;
@@ -859,13 +859,13 @@ void orc_renorm_diags(int P, int D, int m, int n, const int64_t *Cd,
     for (c = 0; c < n; ++c) {
       bigint W, t;
       bi_zero(&W);
-      for (d = 0; d <= D; ++d) {
+      for (d = 0; d < D; ++d) {
         int64_t v = Cd[d * pc + (long)r * n + c];
         if (!v) continue;
-        bi_from_i64_shl(&t, v, 8 * (D - d));
+        bi_from_i64_shl(&t, v, 8 * (D - 1 - d));
         bi_add(&W, &t);
       }
-      to_limbs(P, &W, E[r] + F[c] - 14 - 8 * D, C + ((long)r * n + c) * P);
+      to_limbs(P, &W, E[r] + F[c] - 14 - 8 * (D - 1), C + ((long)r * n + c) * P);
     }
 }
 
@@ -875,7 +875,7 @@ void orc_gemm_slices(int P, int s, int D, int m, int n, int k,
   int *E = (int *)malloc(sizeof(int) * m), *F = (int *)malloc(sizeof(int) * n);
   int *dA = (int *)malloc(sizeof(int) * (size_t)s * m * k);
   int *dB = (int *)malloc(sizeof(int) * (size_t)s * n * k);
-  int64_t *Cd = (int64_t *)malloc(sizeof(int64_t) * (size_t)(D + 1) * m * n);
+  int64_t *Cd = (int64_t *)malloc(sizeof(int64_t) * (size_t)D * m * n);
   orc_scale_exps(P, m, n, k, A, B, E, F);
   orc_digits(P, s, m, k, A, E, 0, dA);
   orc_digits(P, s, n, k, B, F, 1, dB);

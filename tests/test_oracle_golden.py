@@ -99,7 +99,7 @@ def test_slice_digit_form_is_exact_on_small_case(orc, inputs):
     enough bits: qd 16^3 agrees with the exact product to > 212 bits."""
     import oracle.exact as ex
     P, A, B = inputs.workload("qd1024", 16, 16, 16)
-    C = orc.gemm_slices(P, 28, 27, A, B, 16, 16, 16)
+    C = orc.gemm_slices(P, 28, 28, A, B, 16, 16, 16)
     ent, nrm = ex.error_bits(C, A, B, range(16), range(16))
     Cp = orc.gemm_plain(P, A, B, 16, 16, 16)
     ent_p, nrm_p = ex.error_bits(Cp, A, B, range(16), range(16))
