@@ -22,7 +22,7 @@ void set_cuda_error(cudaError_t e) {
 int default_engine() {
   const char *v = std::getenv("MDG_SLICE_ENGINE");
   if (v && *v) return std::atoi(v) ? 1 : 0;
-  return 0;
+  return 1;
 }
 
 // ------------------------------------------------------------------ cache --
