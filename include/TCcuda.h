@@ -22,6 +22,12 @@
 
 #include <stdio.h>
 #include <cuda_runtime.h>
+#ifdef __CUDACC__
+#include <cublas_v2.h>
+#include <curand.h>
+#include <mma.h>
+using namespace nvcuda;  // the reference's drivers use wmma:: unqualified
+#endif
 
 vector<double> mat(int n, int p, int expmin = 0, int expmax = 0);
 vector<double> zeros(int m, int n, int p);

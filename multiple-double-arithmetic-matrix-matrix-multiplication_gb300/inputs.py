@@ -73,6 +73,8 @@ WORKLOADS = {
     "qd1024": (4, 1024, 1024, 1024, 1, "uniform"),
     "od2048_spread": (8, 2048, 2048, 2048, 2, "spread"),
     "qd8192_normal": (4, 8192, 8192, 8192, 4, "normal"),
+    # the headline distribution at 2048^3: the small case for profiling
+    "qd2048_normal": (4, 2048, 2048, 2048, 4, "normal"),
 }
 
 

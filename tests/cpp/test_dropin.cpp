@@ -1,0 +1,52 @@
+// Host-side checks of the drop-in C++ surface (include/TCcuda.h,
+// include/floatybits.h) linked against libmdgemm.so.  Each command reads and
+// writes raw little-endian doubles; tests/test_dropin_cpp.py drives it and
+// compares with the golden vectors made by the reference.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <string>
+
+#include "TCcuda.h"
+
+static vector<double> load(const char *path) {
+  std::ifstream f(path, std::ios::binary | std::ios::ate);
+  const size_t n = (size_t)f.tellg() / sizeof(double);
+  vector<double> v(n);
+  f.seekg(0);
+  f.read(reinterpret_cast<char *>(v.data()), n * sizeof(double));
+  return v;
+}
+
+static void save(const char *path, const vector<double> &v) {
+  std::ofstream f(path, std::ios::binary);
+  f.write(reinterpret_cast<const char *>(v.data()), v.size() * sizeof(double));
+}
+
+int main(int argc, char **argv) {
+  if (argc < 2) return 2;
+  const std::string cmd = argv[1];
+  if (cmd == "mat") {  // mat <n> <p> <seed> <out>
+    srand((unsigned)atoi(argv[4]));
+    save(argv[5], mat(atoi(argv[2]), atoi(argv[3])));
+  } else if (cmd == "matmul") {  // matmul <p> <n> <A> <B> <out>
+    const int p = atoi(argv[2]), n = atoi(argv[3]);
+    vector<double> A = load(argv[4]), B = load(argv[5]), C;
+    if (p == 2) C = matmulddf(A, B, n);
+    else if (p == 4) C = matmulqdf(A, B, n);
+    else if (p == 8) C = matmulodf(A, B, n);
+    else C = matmulhdf(A, B, n);
+    save(argv[6], C);
+  } else if (cmd == "bigB2") {  // bigB2 <n> <pp> <in> <out>
+    save(argv[5], bigB2(load(argv[4]), atoi(argv[2]), atoi(argv[3])));
+  } else if (cmd == "squeeze") {  // squeeze <p> <pp> <in> <out>
+    save(argv[5], pllntsqueeze(load(argv[4]), atoi(argv[2]), atoi(argv[3])));
+  } else if (cmd == "bits") {  // bits <x> : bitform / double_rep round trip
+    const double x = atof(argv[2]);
+    printf("%.17g\n", double_rep(bitform(x)));
+  } else {
+    return 2;
+  }
+  return 0;
+}
