@@ -32,7 +32,8 @@ typedef enum {
   MDG_ERROR_CUDA = 6,           /* a CUDA call failed, see mdg_last_cuda_error() */
   MDG_ERROR_NOT_SUPPORTED = 7,  /* valid request this build cannot serve */
   MDG_ERROR_TIMEOUT = 8,        /* a bounded device-side wait gave up */
-  MDG_ERROR_ALLOCATION = 9      /* device or pinned allocation failed */
+  MDG_ERROR_ALLOCATION = 9,     /* device or pinned allocation failed */
+  MDG_ERROR_TOO_LARGE = 10      /* problem needs more than the fixed scratch of mdg_gemm_slice_static */
 } mdg_status;
 
 /* GEMM forms. */
@@ -114,6 +115,23 @@ int mdg_gemm_batched(int form, const mdg_problem *problems, int count,
                      size_t workspace_bytes, void *stream);
 
 void mdg_release_cache(void);
+
+/* C = A * B in the BF16 slice-digit form (default digits) without any
+ * device allocation and without a workspace argument, for callers that may
+ * not call cudaMalloc: code running inside a stream capture owned by
+ * another component, hosts that own every device allocation, real-time
+ * integrations that forbid allocation after start-up.  No counterpart in
+ * the reference.  The scratch is a fixed array of mdg_static_scratch_bytes()
+ * (64 MiB) inside the library, held on every GPU that loads it; a problem
+ * whose BF16 workspace (mdg_gemm_workspace_size) is larger gets
+ * MDG_ERROR_TOO_LARGE (e.g. quad-double fits up to 512^3, octo-double up to
+ * 256^3).  The first call on a device looks up the array's device address
+ * and should come before any stream capture.  Calls share the array: calls
+ * that overlap on the GPU race, so order them on one stream. */
+size_t mdg_static_scratch_bytes(void);
+int mdg_gemm_slice_static(int p, int m, int n, int k, const double *A, int lda,
+                          const double *B, int ldb, double *C, int ldc,
+                          void *stream);
 
 /* ------------------------------------------------- FP64 split stages -- */
 

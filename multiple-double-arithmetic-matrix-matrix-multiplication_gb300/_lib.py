@@ -51,6 +51,8 @@ SIGNATURES = {
     "mdg_renorm_diagonals": (c_int, [c_int] * 6 + [c_vp, c_ll, c_int, c_vp, c_vp, c_vp, c_int,
                                                    c_vp]),
     "mdg_device_status": (c_int, []),
+    "mdg_static_scratch_bytes": (c_size, []),
+    "mdg_gemm_slice_static": (c_int, [c_int] * 4 + [c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp]),
 }
 
 _lib = None

@@ -175,6 +175,7 @@ const char *mdg_status_string(int status) {
     case MDG_ERROR_NOT_SUPPORTED: return "not supported";
     case MDG_ERROR_TIMEOUT: return "device wait timed out";
     case MDG_ERROR_ALLOCATION: return "allocation failed";
+    case MDG_ERROR_TOO_LARGE: return "problem exceeds the fixed scratch of the allocation-free entry";
   }
   return "unknown status";
 }
