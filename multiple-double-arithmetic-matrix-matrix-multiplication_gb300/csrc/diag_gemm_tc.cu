@@ -23,6 +23,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstdlib>
+
 #include "common.cuh"
 #include "slice_tc.cuh"
 
@@ -341,6 +343,267 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (threadIdx.x == 0 && *abort_flag) atomicExch(&g_tc_error, 1);
 }
 
+// ------------------------------------------------------------------------
+// The same computation on CTA pairs (cta_group::2): a cluster of two CTAs
+// owns a 256 x 256 output tile; CTA r holds rows r*128..+127 of the A
+// k-block and rows r*128..+127 of the B k-block (the N half), and the pair's
+// tensor cores compute M=256 N=256 K=16 per instruction, issued by one thread
+// of the even CTA.  Each CTA streams 32 KiB per k-step instead of 48 and its
+// tensor core reads 8 KiB of operands per 128-cycle MMA instead of 12, which
+// halves the shared-memory traffic that bounds the single-CTA kernel.
+// Synchronisation: both CTAs' TMA loads complete on the even CTA's full
+// barrier (cp.async.bulk.tensor .cta_group::2); the even CTA's MMA commits
+// arrive, multicast, on the empty and accumulator-full barriers of both
+// CTAs; the epilogue warps of both CTAs arrive on the even CTA's
+// accumulator-empty barrier (16 arrivals).  Each CTA's TMEM holds its 128
+// rows of both accumulators.
+constexpr int TN2 = 256, BH = 128;
+constexpr int STAGES2 = 6;
+constexpr int A2_BYTES = TM * TK * 2;  // 16 KiB
+constexpr int B2_BYTES = BH * TK * 2;  // 16 KiB
+constexpr int STAGE2_BYTES = A2_BYTES + B2_BYTES;
+constexpr int SMEM2_BYTES = STAGES2 * STAGE2_BYTES + 1024 + 256;
+constexpr uint32_t IDESC2 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN2 >> 3) << 17) |
+                            ((uint32_t)(256 >> 4) << 24);
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ uint32_t map_to_rank0(uint32_t addr) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, 0;" : "=r"(r) : "r"(addr));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::
+                   : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap *tm, int x, int y,
+                                                 uint32_t bar_cluster) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar_cluster)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16_pair(uint32_t d_tmem, uint64_t a, uint64_t b,
+                                              uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(IDESC2), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar) {
+  const uint16_t mask = 3;
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
+      "[%0], %1;" ::"r"(bar),
+      "h"(mask)
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster)
+               : "memory");
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
+    diag_gemm_tc2_kernel(const __grid_constant__ CUtensorMap tmA,
+                         const __grid_constant__ CUtensorMap tmB, int s, int D, int Mp, int Np,
+                         int KB, int *__restrict__ out, long long plane_c) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES2 * STAGE2_BYTES);
+  // bars: [0,6) full, [6,12) empty, [12,14) accfull, [14,16) accempty, 16 drain
+  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bars + 20);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 21);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = cluster_rank();
+  const bool leader = rank == 0;
+  const uint32_t smem_base = smem_u32(smem);
+  auto full = [&](int st) { return smem_u32(bars + st); };
+  auto empty = [&](int st) { return smem_u32(bars + STAGES2 + st); };
+  auto accfull = [&](int b) { return smem_u32(bars + 2 * STAGES2 + b); };
+  auto accempty = [&](int b) { return smem_u32(bars + 2 * STAGES2 + 2 + b); };
+  const uint32_t drain_bar = smem_u32(bars + 2 * STAGES2 + 4);
+
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < STAGES2; ++st) {
+      mbar_init(full(st), 1);
+      mbar_init(empty(st), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accfull(b), 1);
+      mbar_init(accempty(b), 2 * EPI_WARPS);
+    }
+    mbar_init(drain_bar, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_holder)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  cluster_sync();
+  fence_after();
+  const uint32_t tmem_base = *tmem_holder;
+
+  const int MB = Mp / 256;
+  const int tiles = MB * (Np / TN2);
+  const int cid = blockIdx.x >> 1, ncl = gridDim.x >> 1;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ------------------------------------------------------ producer --
+      int st = 0;
+      uint32_t ph = 0;
+      uint32_t last_par[STAGES2];
+      bool issued[STAGES2];
+      for (int i = 0; i < STAGES2; ++i) issued[i] = false;
+      for (int tile = cid; tile < tiles; tile += ncl) {
+        const int row = (tile % MB) * 256 + (int)rank * TM;
+        const int col = (tile / MB) * TN2 + (int)rank * BH;
+        for (int d = 0; d < D; ++d) {
+          const int ilo = d - (s - 1) > 0 ? d - (s - 1) : 0;
+          const int S = mdgi::diag_pairs(d, s) * KB;
+          for (int t = 0; t < S; ++t) {
+            const int i = ilo + t / KB, kb = t - (t / KB) * KB, j = d - i;
+            if (!mbar_wait(empty(st), ph ^ 1, abort_flag)) goto producer_done;
+            if (leader) mbar_expect_tx(full(st), 2 * STAGE2_BYTES);
+            const uint32_t a_dst = smem_base + st * STAGE2_BYTES;
+            const uint32_t bar0 = map_to_rank0(full(st));
+            tma_load_2d_pair(a_dst, &tmA, kb * TK, i * Mp + row, bar0);
+            tma_load_2d_pair(a_dst + A2_BYTES, &tmB, kb * TK, j * Np + col, bar0);
+            last_par[st] = ph;
+            issued[st] = true;
+            if (++st == STAGES2) {
+              st = 0;
+              ph ^= 1;
+            }
+          }
+        }
+      }
+    producer_done:
+      if (*abort_flag && leader)
+        for (int i = 0; i < STAGES2; ++i)
+          if (issued[i]) mbar_drain(full(i), last_par[i]);
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && leader) {
+      // ---------------------------------------------------- MMA issuer --
+      int st = 0, buf = 0;
+      uint32_t ph = 0, aph[2] = {0, 0};
+      bool any = false;
+      for (int tile = cid; tile < tiles; tile += ncl) {
+        for (int d = 0; d < D; ++d) {
+          const int S = mdgi::diag_pairs(d, s) * KB;
+          for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
+            if (!mbar_wait(accempty(buf), aph[buf] ^ 1, abort_flag)) goto mma_done;
+            fence_after();
+            const uint32_t dt = tmem_base + buf * TN2;
+            const int g1 = g0 + mdgi::GROUP_STEPS < S ? g0 + mdgi::GROUP_STEPS : S;
+            for (int t = g0; t < g1; ++t) {
+              if (!mbar_wait(full(st), ph, abort_flag)) goto mma_done;
+              fence_after();
+              const uint32_t a_addr = smem_base + st * STAGE2_BYTES;
+              const uint64_t da = sw128_desc(a_addr), db = sw128_desc(a_addr + A2_BYTES);
+#pragma unroll
+              for (int kk = 0; kk < TK / 16; ++kk)
+                mma_bf16_pair(dt, da + 2 * kk, db + 2 * kk, (t > g0 || kk > 0) ? 1u : 0u);
+              mma_commit_pair(empty(st));
+              any = true;
+              if (++st == STAGES2) {
+                st = 0;
+                ph ^= 1;
+              }
+            }
+            mma_commit_pair(accfull(buf));
+            aph[buf] ^= 1;
+            buf ^= 1;
+          }
+        }
+      }
+    mma_done:
+      if (*abort_flag && any) {
+        mma_commit_pair(drain_bar);
+        mbar_drain(drain_bar, 0);
+      }
+    }
+  } else {
+    // -------------------------------------------------------- epilogue --
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    int acc[128];
+#pragma unroll
+    for (int j = 0; j < 128; ++j) acc[j] = 0;
+    int buf = 0;
+    uint32_t aph[2] = {0, 0};
+    const uint32_t accempty0[2] = {map_to_rank0(accempty(0)), map_to_rank0(accempty(1))};
+    for (int tile = cid; tile < tiles; tile += ncl) {
+      const int row = (tile % MB) * 256 + (int)rank * TM + 32 * q + lane;
+      const int col = (tile / MB) * TN2 + 128 * h;
+      int chunk = 0;
+      for (int d = 0; d < D; ++d) {
+        const int S = mdgi::diag_pairs(d, s) * KB;
+        for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
+          int ok = 1;
+          if (lane == 0) ok = mbar_wait(accfull(buf), aph[buf], abort_flag) ? 1 : 0;
+          ok = __shfl_sync(0xffffffffu, ok, 0);
+          if (!ok) goto epi_done;
+          aph[buf] ^= 1;
+          fence_after();
+          const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + buf * TN2 + 128 * h;
+#pragma unroll
+          for (int c4 = 0; c4 < 4; ++c4) {
+            uint32_t r[32];
+            tmem_ld32(taddr + 32 * c4, r);
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              acc[32 * c4 + j] += __float_as_int(__uint_as_float(r[j]) + 12582912.0f) - 0x4B400000;
+          }
+          fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive_cluster(accempty0[buf]);
+          buf ^= 1;
+          const int g1 = g0 + mdgi::GROUP_STEPS;
+          if (g1 % mdgi::CHUNK_STEPS == 0 || g1 >= S) {
+            int4 *dst = reinterpret_cast<int4 *>(out + (size_t)chunk * plane_c +
+                                                 (size_t)row * Np + col);
+#pragma unroll
+            for (int v = 0; v < 32; ++v) {
+              dst[v] = make_int4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
+              acc[4 * v] = acc[4 * v + 1] = acc[4 * v + 2] = acc[4 * v + 3] = 0;
+            }
+            ++chunk;
+          }
+        }
+      }
+    }
+  epi_done:;
+  }
+  __syncwarp();
+  fence_before();
+  cluster_sync();
+  fence_after();
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                 "r"(TMEM_COLS)
+                 : "memory");
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(&g_tc_error, 1);
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   if (!fn) {
@@ -380,22 +643,37 @@ int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, co
   if (plane_a != (long long)Mp * Kp || plane_b != (long long)Np * Kp) return MDG_ERROR_INVALID_SIZE;
   if ((reinterpret_cast<uintptr_t>(dA) | reinterpret_cast<uintptr_t>(dB)) & 15)
     return MDG_ERROR_INVALID_SIZE;
+  // the CTA-pair kernel needs 256-row tiles; MDG_TC_PAIR=0 selects the
+  // single-CTA kernel
+  const char *pv = std::getenv("MDG_TC_PAIR");
+  const bool pair = (Mp % 256 == 0) && !(pv && *pv == '0');
   CUtensorMap ma, mb;
   MDG_TRY(make_map(&ma, dA, Kp, (long long)s * Mp, TM));
-  MDG_TRY(make_map(&mb, dB, Kp, (long long)s * Np, TN));
-  static int configured_dev = -1;
+  MDG_TRY(make_map(&mb, dB, Kp, (long long)s * Np, pair ? BH : TN));
+  static int configured_dev[2] = {-1, -1};
   int dev = 0, sms = 0;
   MDG_TRY_CUDA(cudaGetDevice(&dev));
-  if (configured_dev != dev) {
-    MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc_kernel,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    configured_dev = dev;
+  if (configured_dev[pair] != dev) {
+    if (pair)
+      MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc2_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
+    else
+      MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    configured_dev[pair] = dev;
   }
   MDG_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int tiles = (Mp / TM) * (Np / TN);
-  const int grid = tiles < sms ? tiles : sms;
-  diag_gemm_tc_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(ma, mb, s, D, Mp, Np, Kp / TK, chunks,
-                                                         plane_c);
+  if (pair) {
+    const int tiles = (Mp / 256) * (Np / TN2);
+    const int clusters = tiles < sms / 2 ? tiles : sms / 2;
+    diag_gemm_tc2_kernel<<<2 * clusters, THREADS, SMEM2_BYTES, st>>>(ma, mb, s, D, Mp, Np,
+                                                                      Kp / TK, chunks, plane_c);
+  } else {
+    const int tiles = (Mp / TM) * (Np / TN);
+    const int grid = tiles < sms ? tiles : sms;
+    diag_gemm_tc_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(ma, mb, s, D, Mp, Np, Kp / TK, chunks,
+                                                           plane_c);
+  }
   MDG_TRY_LAUNCH();
   return MDG_SUCCESS;
 }

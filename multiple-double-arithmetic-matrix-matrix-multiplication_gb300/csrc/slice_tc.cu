@@ -317,7 +317,7 @@ SlicePlan make_slice_plan(int p, int s, int D, int m, int n, int k) {
   pl.m = m;
   pl.n = n;
   pl.k = k;
-  pl.Mp = (int)align_up(std::max(m, 1), 128);
+  pl.Mp = (int)align_up(std::max(m, 1), 256);
   pl.Np = (int)align_up(std::max(n, 1), 256);
   pl.Kp = (int)align_up(std::max(k, 1), 64);
   pl.chunks = total_chunks(s, D, pl.Kp / 64);

@@ -30,7 +30,7 @@ inline int total_chunks(int s, int D, int KB) {
 // Workspace layout of one slice-digit GEMM (byte offsets, 256-aligned).
 struct SlicePlan {
   int p, s, D, m, n, k;
-  int Mp, Np, Kp;  // padded to 128, 256, 64
+  int Mp, Np, Kp;  // padded to 256, 256, 64
   int chunks;
   long long plane_a, plane_b, plane_c;  // elements between digit / chunk planes
   size_t off_rowbits, off_colbits, off_E, off_F, off_dA, off_dB, off_Cd, total;

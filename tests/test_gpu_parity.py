@@ -188,13 +188,14 @@ def test_digit_stages_bit_exact(api, orc, inputs, P, s):
 
 @pytest.mark.parametrize("engine", ["0", "1"])
 @pytest.mark.parametrize("s,D,k", [(6, 9, 640), (3, 5, 64 * 1100)])
-def test_diagonal_gemm_exact(api, orc, engine, s, D, k, monkeypatch):
+@pytest.mark.parametrize("m,n", [(128, 256), (256, 512)])
+def test_diagonal_gemm_exact(api, orc, engine, s, D, k, m, n, monkeypatch):
     """Digit planes at the extremes the flush interval allows (runs of
     +-128 x -+128 products) through both engines; the second case cuts
-    each diagonal into several int32 chunks."""
+    each diagonal into several int32 chunks.  m = 128 runs the single-CTA
+    tcgen05 kernel, m = 256 the CTA-pair kernel."""
     monkeypatch.setenv("MDG_SLICE_ENGINE", engine)
-    rng = np.random.default_rng(int(engine) + 7 + k)
-    m, n = 128, 256
+    rng = np.random.default_rng(int(engine) + 7 + k + m)
     dA = rng.integers(-128, 129, size=(s, m, k)).astype(np.int32)
     dB = rng.integers(-128, 129, size=(s, n, k)).astype(np.int32)
     dA[:, :, :300] = 128
@@ -223,10 +224,17 @@ def test_renorm_bit_exact(api, orc, P, D, k):
     assert np.array_equal(got, orc.renorm_diags(P, D, diag, E, F, m, n))
 
 
-@pytest.mark.parametrize("engine", ["0", "1"])
+@pytest.mark.parametrize("engine", ["0", "1", "pair0"])
 @pytest.mark.parametrize("P", [2, 4, 8])
-@pytest.mark.parametrize("shape", [(1, 1, 1), (33, 31, 70), (130, 129, 65)])
+@pytest.mark.parametrize("shape", [(1, 1, 1), (33, 31, 70), (130, 129, 65), (300, 260, 130)])
 def test_slice_gemm_bit_exact_against_oracle(api, orc, inputs, engine, P, shape, monkeypatch):
+    """engine 0: mma.sync; 1: tcgen05 CTA pairs (the default); pair0:
+    tcgen05 single CTA."""
+    if engine == "pair0":
+        monkeypatch.setenv("MDG_TC_PAIR", "0")
+        engine = "1"
+    if P == 8 and shape[0] * shape[1] * shape[2] > 3e6:
+        pytest.skip("oracle cost")
     monkeypatch.setenv("MDG_SLICE_ENGINE", engine)
     m, n, k = shape
     rng = np.random.default_rng(m + n + k + P)
