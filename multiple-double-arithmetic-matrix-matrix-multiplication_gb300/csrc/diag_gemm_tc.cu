@@ -3,7 +3,7 @@
 // For every output tile (128 rows x 256 columns) and every diagonal d < D,
 // the products A_i B_j^T with i + j = d are summed over k exactly: BF16
 // digits in [-128, 128], FP32 accumulation in tensor memory (TMEM), flushed
-// every 256 products (|partial| <= 2^22) into int32 registers, stored every
+// every 1024 products (|partial| <= 2^24) into int32 registers, stored every
 // 65536 products as one int32 chunk plane (|sum| <= 2^30).
 //
 // One CTA per SM, persistent over tiles; 10 warps with fixed roles:
@@ -13,9 +13,9 @@
 //               M=128 N=256 K=16, BF16 x BF16 -> FP32, into one of two
 //               256-column accumulators (all 512 TMEM columns),
 //   warps 2-9   epilogue: tcgen05.ld of the accumulator (warp w reads TMEM
-//               lanes 32 (w % 4) .. +31, columns 128 ((w - 2) / 4) .. +127),
-//               exact float -> int conversion, int32 accumulation, chunk
-//               stores.
+//               lanes 32 (w % 4) .. +31, columns 128 ((w - 2) / 4) .. +127)
+//               every 16 k-steps, exact float -> int conversion, int32
+//               accumulation, chunk stores.
 // Barriers: full/empty per stage (TMA <-> MMA), accfull/accempty per
 // accumulator (MMA <-> epilogue).  Every wait is bounded (2 s of
 // %globaltimer); on a timeout the CTA records the error, stops issuing,
@@ -143,6 +143,7 @@ __device__ __forceinline__ void fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
+// Asynchronous TMEM load of 32 columns of this warp's 32 lanes.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
@@ -154,7 +155,46 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
         "=r"(r[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Waits for this thread's outstanding TMEM loads.  The registers of the
+// last load are operands, so no read of them can move above the wait.
+__device__ __forceinline__ void tmem_wait(uint32_t (&r)[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]),
+                 "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
+                 "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]),
+                 "+r"(r[30]), "+r"(r[31])
+               :
+               : "memory");
+}
+
+// The accumulator holds integer-valued floats with |x| <= 2^24; the
+// conversion to int32 is exact.
+__device__ __forceinline__ void add_exact(int *acc, const uint32_t (&r)[32]) {
+#pragma unroll
+  for (int j = 0; j < 32; ++j) acc[j] += __float2int_rn(__uint_as_float(r[j]));
+}
+
+// Adds 128 accumulator columns (starting at taddr) into acc: four 32-column
+// loads, each issued before the previous block is converted so that the
+// load latency overlaps the integer work.
+__device__ __forceinline__ void drain128(uint32_t taddr, int (&acc)[128]) {
+  uint32_t ra[32], rb[32];
+  tmem_ld32(taddr, ra);
+  tmem_wait(ra);
+  tmem_ld32(taddr + 32, rb);
+  add_exact(acc, ra);
+  tmem_wait(rb);
+  tmem_ld32(taddr + 64, ra);
+  add_exact(acc + 32, rb);
+  tmem_wait(ra);
+  tmem_ld32(taddr + 96, rb);
+  add_exact(acc + 64, ra);
+  tmem_wait(rb);
+  add_exact(acc + 96, rb);
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
@@ -304,14 +344,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           aph[buf] ^= 1;
           fence_after();
           const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + buf * TN + 128 * h;
-#pragma unroll
-          for (int c4 = 0; c4 < 4; ++c4) {
-            uint32_t r[32];
-            tmem_ld32(taddr + 32 * c4, r);
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-              acc[32 * c4 + j] += __float_as_int(__uint_as_float(r[j]) + 12582912.0f) - 0x4B400000;
-          }
+          drain128(taddr, acc);
           fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(accempty(buf));
@@ -565,14 +598,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
           aph[buf] ^= 1;
           fence_after();
           const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + buf * TN2 + 128 * h;
-#pragma unroll
-          for (int c4 = 0; c4 < 4; ++c4) {
-            uint32_t r[32];
-            tmem_ld32(taddr + 32 * c4, r);
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-              acc[32 * c4 + j] += __float_as_int(__uint_as_float(r[j]) + 12582912.0f) - 0x4B400000;
-          }
+          drain128(taddr, acc);
           fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive_cluster(accempty0[buf]);

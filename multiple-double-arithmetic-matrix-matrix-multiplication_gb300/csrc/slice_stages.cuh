@@ -1,0 +1,208 @@
+// Per-element / per-block bodies of the slice-digit stage kernels, shared
+// by the single-problem kernels (slice_tc.cu) and the batched kernels
+// (batched.cu).  See slice_tc.cu for what each stage computes.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "slice_common.cuh"
+#include "slice_tc.cuh"
+
+namespace mdgi {
+
+// ------------------------------------------------------------ exponents --
+// Block 32 x 8 covers 32 columns x 256 rows; each warp walks 32 rows of
+// one 32-column strip.  Row maxima: warp reduction, one atomic per row per
+// warp.  Column maxima: one atomic per thread.  Maxima of non-negative
+// doubles are compared as 64-bit integers.
+__device__ __forceinline__ void absmax_block(int P, int R, int Cn, const double *__restrict__ X,
+                                             int ldx, unsigned long long *rowbits,
+                                             unsigned long long *colbits, int bx, int by) {
+  const int c = bx * 32 + threadIdx.x;
+  const int r0 = by * 256 + threadIdx.y * 32;
+  double cm = 0.0;
+  for (int rr = 0; rr < 32; ++rr) {
+    const int r = r0 + rr;
+    if (r >= R) break;
+    double v = 0.0;
+    if (c < Cn) {
+      const double *x = X + ((size_t)r * ldx + c) * P;
+      v = fabs(x[0]);
+      for (int l = 1; l < P; ++l) v = v + fabs(x[l]);
+    }
+    cm = fmax(cm, v);
+    if (rowbits) {
+      double w = v;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) w = fmax(w, __shfl_xor_sync(0xffffffffu, w, o));
+      if (threadIdx.x == 0) atomicMax(rowbits + r, (unsigned long long)__double_as_longlong(w));
+    }
+  }
+  if (colbits && c < Cn) atomicMax(colbits + c, (unsigned long long)__double_as_longlong(cm));
+}
+
+// --------------------------------------------------------------- digits --
+// One thread per element of the padded plane (prow, pcol); pcol (the k
+// index) is the fastest, so plane stores are coalesced.  Outside the valid
+// region every digit is zero.
+template <int NW>
+__device__ __forceinline__ void digits_elem(int P, int s, int rows, int cols,
+                                            const double *__restrict__ X, int ldx,
+                                            const int *__restrict__ E, int trans,
+                                            __nv_bfloat16 *__restrict__ planes, int ld_out,
+                                            long long plane_stride, int rows_pad, int cols_pad,
+                                            int pr, int pc) {
+  if (pc >= cols_pad || pr >= rows_pad) return;
+  __nv_bfloat16 *out = planes + (size_t)pr * ld_out + pc;
+  if (pr >= rows || pc >= cols) {
+    for (int i = 0; i < s; ++i) out[i * plane_stride] = __float2bfloat16_rn(0.0f);
+    return;
+  }
+  const double *a = trans ? X + ((size_t)pc * ldx + pr) * P : X + ((size_t)pr * ldx + pc) * P;
+  const int S = 7 + 8 * (s - 1);
+  const int Er = E[pr];
+  uint64_t w[NW];
+#pragma unroll
+  for (int i = 0; i < NW; ++i) w[i] = 0;
+  for (int l = 0; l < P; ++l) {
+    const double x = a[l];
+    if (x == 0.0) continue;
+    int e;
+    const double f = frexp(x, &e);
+    const int64_t m = (int64_t)ldexp(f, 53);
+    const int q = e - 53 + S - Er;
+    if (q >= 0) {
+      mdgi::wide_add_shifted<NW>(w, m, q);
+    } else if (q > -64) {
+      mdgi::wide_add_shifted<NW>(w, m >> (-q), 0);
+    } else {
+      mdgi::wide_add_shifted<NW>(w, m < 0 ? -1 : 0, 0);
+    }
+  }
+  // balanced digits from the bottom: t = byte + carry, t >= 128 -> t - 256
+  int carry = 0;
+#pragma unroll
+  for (int wi = 0; wi < NW; ++wi) {
+    const uint64_t word = w[wi];
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int p = wi * 8 + b;
+      if (p < s - 1) {
+        const int t = (int)((word >> (8 * b)) & 255) + carry;
+        const int d = t >= 128 ? t - 256 : t;
+        carry = t >= 128 ? 1 : 0;
+        out[(s - 1 - p) * plane_stride] = __float2bfloat16_rn((float)d);
+      }
+    }
+  }
+  const int top = (int)(int64_t)mdgi::wide_bits64<NW>(w, 8 * (s - 1)) + carry;
+  out[0] = __float2bfloat16_rn((float)top);
+}
+
+// --------------------------------------------------------------- renorm --
+// W = sum_d C_d 256^(D-1-d) is built bottom-up (Horner from the least
+// significant diagonal): T = C_{D-1}; repeatedly emit the low byte of T as
+// the next byte of W and continue with floor(T / 256) + C_{d-1}; after
+// diagonal 0, T is the top part of W, above bit 8 (D - 1).  The emitted
+// bytes land at positions fixed at compile time, so W stays in registers.
+// Each thread takes V adjacent columns and loads their chunk sums as one
+// vector per chunk plane.
+template <int V>
+struct IntV;
+template <>
+struct IntV<4> {
+  static __device__ __forceinline__ void load(const int *p, int (&x)[4]) {
+    const int4 t = *reinterpret_cast<const int4 *>(p);
+    x[0] = t.x; x[1] = t.y; x[2] = t.z; x[3] = t.w;
+  }
+};
+template <>
+struct IntV<2> {
+  static __device__ __forceinline__ void load(const int *p, int (&x)[2]) {
+    const int2 t = *reinterpret_cast<const int2 *>(p);
+    x[0] = t.x; x[1] = t.y;
+  }
+};
+template <>
+struct IntV<1> {
+  static __device__ __forceinline__ void load(const int *p, int (&x)[1]) { x[0] = *p; }
+};
+
+template <int P, int NW, int V>
+__device__ __forceinline__ void renorm_elems(int s, int D, int KB, int m, int n,
+                                             const int *__restrict__ chunks, long long plane_c,
+                                             int ldcd, const int *__restrict__ E,
+                                             const int *__restrict__ F, double *__restrict__ C,
+                                             int ldc, int r, int c0) {
+  if (c0 >= n || r >= m) return;
+  const int *src = chunks + (size_t)r * ldcd + c0;
+  int q = 0;
+  for (int d = 0; d < D; ++d) q += mdgi::diag_chunks(d, s, KB);
+  uint64_t w[V][NW];
+  long long T[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    T[v] = 0;
+#pragma unroll
+    for (int i = 0; i < NW; ++i) w[v][i] = 0;
+  }
+#pragma unroll
+  for (int wi = 0; wi < NW; ++wi) {
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int k = wi * 8 + b;
+      if (k < D) {
+        const int d = D - 1 - k;
+        const int nc = mdgi::diag_chunks(d, s, KB);
+        q -= nc;
+        for (int j = 0; j < nc; ++j) {
+          int x[V];
+          IntV<V>::load(src + (size_t)(q + j) * plane_c, x);
+#pragma unroll
+          for (int v = 0; v < V; ++v) T[v] += x[v];
+        }
+        if (k < D - 1) {
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            w[v][wi] |= (uint64_t)(T[v] & 255) << (8 * b);
+            T[v] >>= 8;
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const int c = c0 + v;
+    if (c >= n) break;
+    mdgi::wide_add_shifted<NW>(w[v], T[v], 8 * (D - 1));
+    const int scale = E[r] + F[c] - 14 - 8 * (D - 1);
+    double *out = C + ((size_t)r * ldc + c) * P;
+#pragma unroll 1
+    for (int l = 0; l < P; ++l) {
+      const bool neg = (int64_t)w[v][NW - 1] < 0;
+      uint64_t mag[NW];
+#pragma unroll
+      for (int i = 0; i < NW; ++i) mag[i] = w[v][i];
+      if (neg) mdgi::wide_neg<NW>(mag);
+      const int tb = mdgi::wide_msb<NW>(mag);
+      if (tb < 0) {
+        out[l] = 0.0;
+        continue;
+      }
+      const int sh = tb > 52 ? tb - 52 : 0;
+      uint64_t mm = mdgi::wide_bits64<NW>(mag, sh) & ((1ull << 53) - 1);
+      if (sh > 0) {
+        const bool rb = (mdgi::wide_bits64<NW>(mag, sh - 1) & 1ull) != 0;
+        const bool sticky = sh > 1 && mdgi::wide_any_below<NW>(mag, sh - 1);
+        if (rb && (sticky || (mm & 1))) mm += 1;
+      }
+      const double val = ldexp((double)mm, sh + scale);
+      out[l] = neg ? -val : val;
+      mdgi::wide_add_shifted<NW>(w[v], neg ? (int64_t)mm : -(int64_t)mm, sh);
+    }
+  }
+}
+
+}  // namespace mdgi

@@ -11,8 +11,9 @@
 //    B's are transposed to n x k so both operands are K-major.
 // 3. diagonal GEMM.  C_d = sum_{i+j=d} A_i B_j^T for d < D.  One product
 //    of two digits is at most 2^14, so an FP32 accumulator holds the exact
-//    sum of 256 of them (|sum| <= 2^22); every 256 products the FP32
-//    accumulator is flushed into 32-bit integers, and every 65536 products
+//    sum of 1024 of them (|sum| <= 2^24); every 1024 products (256 in the
+//    mma.sync engine) the FP32 accumulator is flushed into 32-bit
+//    integers, and every 65536 products
 //    the integers are stored as one "chunk" plane (|sum| <= 2^30).  All
 //    sums are exact.
 // 4. renormalisation.  W = sum_d C_d 256^(D-1-d), C_d the sum of the
@@ -26,6 +27,7 @@
 #include "common.cuh"
 #include "slice_common.cuh"
 #include "slice_tc.cuh"
+#include "slice_stages.cuh"
 
 #include <cuda_bf16.h>
 
@@ -34,33 +36,9 @@ namespace {
 using mdgi::wide_add_shifted;
 
 // ------------------------------------------------------------ exponents --
-// Block 32 x 8 covers 32 columns x 256 rows; each warp walks 32 rows of
-// one 32-column strip.  Row maxima: warp reduction, one atomic per row per
-// warp.  Column maxima: one atomic per thread.  Maxima of non-negative
-// doubles are compared as 64-bit integers.
 __global__ void absmax_kernel(int P, int R, int Cn, const double *__restrict__ X, int ldx,
                               unsigned long long *rowbits, unsigned long long *colbits) {
-  const int c = blockIdx.x * 32 + threadIdx.x;
-  const int r0 = blockIdx.y * 256 + threadIdx.y * 32;
-  double cm = 0.0;
-  for (int rr = 0; rr < 32; ++rr) {
-    const int r = r0 + rr;
-    if (r >= R) break;
-    double v = 0.0;
-    if (c < Cn) {
-      const double *x = X + ((size_t)r * ldx + c) * P;
-      v = fabs(x[0]);
-      for (int l = 1; l < P; ++l) v = v + fabs(x[l]);
-    }
-    cm = fmax(cm, v);
-    if (rowbits) {
-      double w = v;
-#pragma unroll
-      for (int o = 16; o; o >>= 1) w = fmax(w, __shfl_xor_sync(0xffffffffu, w, o));
-      if (threadIdx.x == 0) atomicMax(rowbits + r, (unsigned long long)__double_as_longlong(w));
-    }
-  }
-  if (colbits && c < Cn) atomicMax(colbits + c, (unsigned long long)__double_as_longlong(cm));
+  mdgi::absmax_block(P, R, Cn, X, ldx, rowbits, colbits, blockIdx.x, blockIdx.y);
 }
 
 __global__ void exps_kernel(int count, const unsigned long long *__restrict__ bits,
@@ -70,67 +48,22 @@ __global__ void exps_kernel(int count, const unsigned long long *__restrict__ bi
 }
 
 // --------------------------------------------------------------- digits --
-// One thread per element of the padded plane (prow, pcol); pcol (the k
-// index) is the fastest, so plane stores are coalesced.  Outside the valid
-// region every digit is zero.
 template <int NW>
 __global__ void digits_kernel(int P, int s, int rows, int cols, const double *__restrict__ X,
                               int ldx, const int *__restrict__ E, int trans,
                               __nv_bfloat16 *__restrict__ planes, int ld_out,
                               long long plane_stride, int rows_pad, int cols_pad) {
-  const int pc = blockIdx.x * blockDim.x + threadIdx.x;
-  const int pr = blockIdx.y;
-  if (pc >= cols_pad || pr >= rows_pad) return;
-  __nv_bfloat16 *out = planes + (size_t)pr * ld_out + pc;
-  if (pr >= rows || pc >= cols) {
-    for (int i = 0; i < s; ++i) out[i * plane_stride] = __float2bfloat16_rn(0.0f);
-    return;
-  }
-  const double *a = trans ? X + ((size_t)pc * ldx + pr) * P : X + ((size_t)pr * ldx + pc) * P;
-  const int S = 7 + 8 * (s - 1);
-  const int Er = E[pr];
-  uint64_t w[NW];
-#pragma unroll
-  for (int i = 0; i < NW; ++i) w[i] = 0;
-  for (int l = 0; l < P; ++l) {
-    const double x = a[l];
-    if (x == 0.0) continue;
-    int e;
-    const double f = frexp(x, &e);
-    const int64_t m = (int64_t)ldexp(f, 53);
-    const int q = e - 53 + S - Er;
-    if (q >= 0) {
-      wide_add_shifted<NW>(w, m, q);
-    } else if (q > -64) {
-      wide_add_shifted<NW>(w, m >> (-q), 0);
-    } else {
-      wide_add_shifted<NW>(w, m < 0 ? -1 : 0, 0);
-    }
-  }
-  // balanced digits from the bottom: t = byte + carry, t >= 128 -> t - 256
-  int carry = 0;
-#pragma unroll
-  for (int wi = 0; wi < NW; ++wi) {
-    const uint64_t word = w[wi];
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-      const int p = wi * 8 + b;
-      if (p < s - 1) {
-        const int t = (int)((word >> (8 * b)) & 255) + carry;
-        const int d = t >= 128 ? t - 256 : t;
-        carry = t >= 128 ? 1 : 0;
-        out[(s - 1 - p) * plane_stride] = __float2bfloat16_rn((float)d);
-      }
-    }
-  }
-  const int top = (int)(int64_t)mdgi::wide_bits64<NW>(w, 8 * (s - 1)) + carry;
-  out[0] = __float2bfloat16_rn((float)top);
+  mdgi::digits_elem<NW>(P, s, rows, cols, X, ldx, E, trans, planes, ld_out, plane_stride,
+                        rows_pad, cols_pad, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------- diagonal GEMM v0 --
 // mma.sync m16n8k16 BF16 -> FP32.  Block 128 x 64, 8 warps as 4 x 2, warp
 // tile 32 x 32 (2 x 4 MMA tiles), K chunk 32 through shared memory.
 constexpr int BM = 128, BN = 64, BK = 32, SK = BK + 8;
+// k-steps of 64 per FP32 flush in this engine: 256 products, |sum| <= 2^22,
+// the range of the exact_int conversion below
+constexpr int V0_GROUP_STEPS = 4;
 
 __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4],
                                          const uint32_t (&b)[2]) {
@@ -215,7 +148,7 @@ __global__ void __launch_bounds__(256)
         }
         __syncthreads();
       }
-      const bool group_end = (step % mdgi::GROUP_STEPS == mdgi::GROUP_STEPS - 1) || step == S - 1;
+      const bool group_end = (step % V0_GROUP_STEPS == V0_GROUP_STEPS - 1) || step == S - 1;
       const bool chunk_end = (step % mdgi::CHUNK_STEPS == mdgi::CHUNK_STEPS - 1) || step == S - 1;
       if (group_end) {
 #pragma unroll
@@ -249,49 +182,13 @@ __global__ void __launch_bounds__(256)
 }
 
 // --------------------------------------------------------------- renorm --
-template <int P, int NW>
-__global__ void renorm_kernel(int s, int D, int KB, int m, int n, const int *__restrict__ chunks,
-                              long long plane_c, int ldcd, const int *__restrict__ E,
-                              const int *__restrict__ F, double *__restrict__ C, int ldc) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  const int r = blockIdx.y;
-  if (c >= n || r >= m) return;
-  uint64_t w[NW];
-#pragma unroll
-  for (int i = 0; i < NW; ++i) w[i] = 0;
-  const int *src = chunks + (size_t)r * ldcd + c;
-  int q = 0;
-  for (int d = 0; d < D; ++d) {
-    long long v = 0;
-    const int nc = mdgi::diag_chunks(d, s, KB);
-    for (int j = 0; j < nc; ++j, ++q) v += src[q * plane_c];
-    if (v) wide_add_shifted<NW>(w, v, 8 * (D - 1 - d));
-  }
-  const int scale = E[r] + F[c] - 14 - 8 * (D - 1);
-  double *out = C + ((size_t)r * ldc + c) * P;
-#pragma unroll 1
-  for (int l = 0; l < P; ++l) {
-    const bool neg = (int64_t)w[NW - 1] < 0;
-    uint64_t mag[NW];
-#pragma unroll
-    for (int i = 0; i < NW; ++i) mag[i] = w[i];
-    if (neg) mdgi::wide_neg<NW>(mag);
-    const int tb = mdgi::wide_msb<NW>(mag);
-    if (tb < 0) {
-      out[l] = 0.0;
-      continue;
-    }
-    const int sh = tb > 52 ? tb - 52 : 0;
-    uint64_t mm = mdgi::wide_bits64<NW>(mag, sh) & ((1ull << 53) - 1);
-    if (sh > 0) {
-      const bool rb = (mdgi::wide_bits64<NW>(mag, sh - 1) & 1ull) != 0;
-      const bool sticky = sh > 1 && mdgi::wide_any_below<NW>(mag, sh - 1);
-      if (rb && (sticky || (mm & 1))) mm += 1;
-    }
-    const double v = ldexp((double)mm, sh + scale);
-    out[l] = neg ? -v : v;
-    wide_add_shifted<NW>(w, neg ? (int64_t)mm : -(int64_t)mm, sh);
-  }
+template <int P, int NW, int V>
+__global__ void __launch_bounds__(128)
+    renorm_kernel(int s, int D, int KB, int m, int n, const int *__restrict__ chunks,
+                  long long plane_c, int ldcd, const int *__restrict__ E,
+                  const int *__restrict__ F, double *__restrict__ C, int ldc) {
+  mdgi::renorm_elems<P, NW, V>(s, D, KB, m, n, chunks, plane_c, ldcd, E, F, C, ldc, blockIdx.y,
+                               (blockIdx.x * blockDim.x + threadIdx.x) * V);
 }
 
 }  // namespace
@@ -407,15 +304,29 @@ int launch_renorm(int p, int s, int D, int KB, int m, int n, const int *chunks,
   if (m == 0 || n == 0) return MDG_SUCCESS;
   const int NW = words_for(1, D);
   if (!NW) return MDG_ERROR_NOT_SUPPORTED;
-  dim3 grid(ceil_div(n, 128), m);
-#define MDG_RENORM(PP, W)                                                                  \
-  renorm_kernel<PP, W><<<grid, 128, 0, st>>>(s, D, KB, m, n, chunks, plane_c, ldcd, E, F, C, ldc)
-#define MDG_RENORM_P(PP)           \
-  switch (NW) {                    \
-    case 4: MDG_RENORM(PP, 4); break;  \
-    case 6: MDG_RENORM(PP, 6); break;  \
-    case 10: MDG_RENORM(PP, 10); break; \
-    default: MDG_RENORM(PP, 16); break; \
+  // V adjacent columns per thread need V-aligned rows of chunk planes
+  const int Vmax = NW <= 6 ? 4 : NW <= 10 ? 2 : 1;
+  int V = Vmax;
+  while (V > 1 && ((ldcd % V) || (plane_c % V) ||
+                   (reinterpret_cast<uintptr_t>(chunks) % (4 * V))))
+    V >>= 1;
+#define MDG_RENORM(PP, W, VV)                                                              \
+  renorm_kernel<PP, W, VV><<<dim3(ceil_div(ceil_div(n, VV), 128), m), 128, 0, st>>>(      \
+      s, D, KB, m, n, chunks, plane_c, ldcd, E, F, C, ldc)
+#define MDG_RENORM_V(PP, W)          \
+  if (V == 4 && W <= 6) {            \
+    MDG_RENORM(PP, W, 4);            \
+  } else if (V >= 2 && W <= 10) {    \
+    MDG_RENORM(PP, W, 2);            \
+  } else {                           \
+    MDG_RENORM(PP, W, 1);            \
+  }
+#define MDG_RENORM_P(PP)                    \
+  switch (NW) {                             \
+    case 4: MDG_RENORM_V(PP, 4); break;     \
+    case 6: MDG_RENORM_V(PP, 6); break;     \
+    case 10: MDG_RENORM_V(PP, 10); break;   \
+    default: MDG_RENORM_V(PP, 16); break;   \
   }
   switch (p) {
     case 2: MDG_RENORM_P(2); break;
@@ -425,6 +336,7 @@ int launch_renorm(int p, int s, int D, int KB, int m, int n, const int *chunks,
     default: return MDG_ERROR_INVALID_LIMBS;
   }
 #undef MDG_RENORM_P
+#undef MDG_RENORM_V
 #undef MDG_RENORM
   MDG_TRY_LAUNCH();
   return MDG_SUCCESS;

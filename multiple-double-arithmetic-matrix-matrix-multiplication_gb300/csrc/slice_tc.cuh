@@ -12,7 +12,10 @@ namespace mdgi {
 // so every chunk sum is an exact int32 with |sum| <= 2^30.  Chunks are
 // numbered diagonal by diagonal.
 constexpr int CHUNK_STEPS = 1024;
-constexpr int GROUP_STEPS = 4;  // k-steps per FP32 flush: 256 products, |sum| <= 2^22
+// k-steps of 64 per FP32 accumulator flush in the tcgen05 engines: 1024
+// products of magnitude <= 2^14, so every partial sum is an integer with
+// |sum| <= 2^24, exactly representable in FP32.
+constexpr int GROUP_STEPS = 16;
 
 __host__ __device__ inline int diag_pairs(int d, int s) {
   const int lo = d - (s - 1) > 0 ? d - (s - 1) : 0, hi = d < s - 1 ? d : s - 1;

@@ -198,8 +198,11 @@ def test_diagonal_gemm_exact(api, orc, engine, s, D, k, m, n, monkeypatch):
     rng = np.random.default_rng(int(engine) + 7 + k + m)
     dA = rng.integers(-128, 129, size=(s, m, k)).astype(np.int32)
     dB = rng.integers(-128, 129, size=(s, n, k)).astype(np.int32)
-    dA[:, :, :300] = 128
-    dB[:, :, :300] = -128
+    # a run of 1100 products of -2^14 fills one FP32 flush group of 1024
+    # products to exactly -2^24 (the bound of the tcgen05 engines)
+    run = min(k, 1100)
+    dA[:, :, :run] = 128
+    dB[:, :, :run] = -128
     ref = orc.diag_sums(s, D, dA, dB, m, n, k)
     Cd = api.slice_diagonals(dev(dA).to(torch.bfloat16), dev(dB).to(torch.bfloat16), D)
     assert np.array_equal(api.chunks_to_diagonals(Cd, s, D, k), ref)
