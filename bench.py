@@ -43,6 +43,7 @@ UNIT = "GFLOP/s"
 WORKLOADS = {
     "qd8192_normal": "qd8192_normal",
     "qd2048_normal": "qd2048_normal",
+    "qd4096_normal": "qd4096_normal",
     "qd1024": "qd1024",
     "od2048_spread": "od2048_spread",
     "dd64": "dd64",

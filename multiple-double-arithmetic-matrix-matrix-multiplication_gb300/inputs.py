@@ -75,6 +75,7 @@ WORKLOADS = {
     "qd8192_normal": (4, 8192, 8192, 8192, 4, "normal"),
     # the headline distribution at 2048^3: the small case for profiling
     "qd2048_normal": (4, 2048, 2048, 2048, 4, "normal"),
+    "qd4096_normal": (4, 4096, 4096, 4096, 4, "normal"),
 }
 
 
