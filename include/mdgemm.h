@@ -116,6 +116,22 @@ int mdg_gemm_batched(int form, const mdg_problem *problems, int count,
 
 void mdg_release_cache(void);
 
+/* Batched BF16 slice-digit GEMM as a reusable plan.  mdg_batch_create lays
+ * out `workspace` (mdg_batch_workspace_size bytes) for these problems
+ * (device pointers, P in {2,4,8,16}, m, n, k >= 1, default digits per P),
+ * uploads the per-problem tables and tensor maps and returns a handle;
+ * it synchronises `stream`.  mdg_batch_run only launches kernels (8 per
+ * batch: exponents, digits, one grouped tcgen05 diagonal GEMM over the
+ * tiles of every problem, renormalisation) and may be captured into a CUDA
+ * graph; each C equals the single-problem mdg_gemm result bit for bit.  No
+ * counterpart in the reference. */
+typedef struct mdg_batch_s *mdg_batch;
+size_t mdg_batch_workspace_size(const mdg_problem *problems, int count);
+int mdg_batch_create(const mdg_problem *problems, int count, void *workspace,
+                     size_t workspace_bytes, void *stream, mdg_batch *out);
+int mdg_batch_run(mdg_batch batch, void *stream);
+void mdg_batch_destroy(mdg_batch batch);
+
 /* C = A * B in the BF16 slice-digit form (default digits) without any
  * device allocation and without a workspace argument, for callers that may
  * not call cudaMalloc: code running inside a stream capture owned by

@@ -52,6 +52,10 @@ SIGNATURES = {
                                                    c_vp]),
     "mdg_device_status": (c_int, []),
     "mdg_static_scratch_bytes": (c_size, []),
+    "mdg_batch_workspace_size": (c_size, [_P_PROB, c_int]),
+    "mdg_batch_create": (c_int, [_P_PROB, c_int, c_vp, c_size, c_vp, ctypes.POINTER(c_vp)]),
+    "mdg_batch_run": (c_int, [c_vp, c_vp]),
+    "mdg_batch_destroy": (None, [c_vp]),
     "mdg_gemm_slice_static": (c_int, [c_int] * 4 + [c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp]),
 }
 

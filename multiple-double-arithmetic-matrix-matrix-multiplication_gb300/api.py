@@ -101,6 +101,40 @@ def gemm_batched(problems, form="plain", stream=None, **kw):
     return Cs
 
 
+class BatchPlan:
+    """A batched BF16 slice-digit GEMM over fixed device operands: the
+    tables are uploaded once (mdg_batch_create); run() only launches
+    kernels, so it can be captured into a CUDA graph."""
+
+    def __init__(self, problems, stream=None):
+        self.Cs, self.keep = [], []
+        table = (Problem * len(problems))()
+        for i, (A, B) in enumerate(problems):
+            m, k, p = A.shape
+            n = B.shape[1]
+            A, B = A.contiguous(), B.contiguous()
+            C = torch.empty((m, n, p), dtype=torch.float64, device=A.device)
+            self.keep += [A, B]
+            self.Cs.append(C)
+            table[i] = Problem(p, m, n, k, A.data_ptr(), B.data_ptr(), C.data_ptr(), k, n, n)
+        self.table = table
+        need = lib().mdg_batch_workspace_size(table, len(problems))
+        self.ws = torch.empty(max(need, 1), dtype=torch.uint8, device="cuda")
+        h = ctypes.c_void_p()
+        check(lib().mdg_batch_create(table, len(problems), _ptr(self.ws), need, _stream(stream),
+                                     ctypes.byref(h)), "mdg_batch_create")
+        self.handle = h
+
+    def run(self, stream=None):
+        check(lib().mdg_batch_run(self.handle, _stream(stream)), "mdg_batch_run")
+        return self.Cs
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            lib().mdg_batch_destroy(self.handle)
+            self.handle = None
+
+
 # --------------------------------------------------- reference-named API --
 
 def matmulTCnt(A, B, n, nfrag, p, loop_ct=1):

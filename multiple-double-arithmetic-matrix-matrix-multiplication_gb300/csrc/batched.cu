@@ -1,0 +1,330 @@
+// Batched slice-digit GEMM: many problems of uneven m, n, k and mixed P in
+// one launch per stage.
+//
+// mdg_batch_create lays out the caller's workspace (a table of problems,
+// the scale-exponent arrays of all problems side by side, every problem's
+// digit and chunk planes) and uploads the tables, tensor maps included;
+// mdg_batch_run only launches kernels, so it can be captured into a CUDA
+// graph and replayed:
+//   memset of the row / column maxima
+//   absmax over the rows of every A, absmax over the columns of every B
+//   exponents of all rows and columns
+//   digits of every A, digits of every B
+//   one grouped tcgen05 diagonal GEMM over the tiles of all problems
+//   renormalisation of every C
+// Each stage kernel finds its problem from its block index by binary search
+// over per-problem prefix counts.  Digit and renorm kernels use the widest
+// integer the batch needs for every problem (a wider integer gives the same
+// bits).  Each problem's result equals the single-problem mdg_gemm result
+// bit for bit.  The reference runs one square problem per call; it has no
+// counterpart of this entry.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "slice_stages.cuh"
+#include "slice_tc.cuh"
+
+namespace mdgi {
+
+struct BatchProblem {
+  int p, s, D, m, n, k, Mp, Np, Kp;
+  const double *A, *B;
+  double *C;
+  int lda, ldb, ldc;
+  int offE, offF;  // row maxima / exponents of A at offE, of B's columns at offF
+  __nv_bfloat16 *dA, *dB;
+  int *chunks;
+  long long plane_a, plane_b, plane_c;
+  int rowblk_begin;  // absmax of A: blocks of 256 rows
+  int colblk_begin;  // absmax of B: blocks of 256 rows of B (k)
+  int digA_begin;    // digits of A: rows Mp
+  int digB_begin;    // digits of B: rows Np
+  int out_begin;     // renorm: rows m
+};
+
+}  // namespace mdgi
+
+struct mdg_batch_s {
+  int count = 0, nw = 4, total_tiles = 0;
+  int total_rowblk = 0, total_colblk = 0, total_digA = 0, total_digB = 0, total_out = 0;
+  int max_k = 0, max_n = 0, max_Kp = 0;
+  int total_exps = 0;
+  mdgi::BatchProblem *dprobs = nullptr;
+  mdgi::GroupedProblem *dgroups = nullptr;
+  unsigned long long *bits = nullptr;  // row maxima then column maxima
+  int *exps = nullptr;                 // E of all problems then F
+};
+
+namespace {
+
+using mdgi::BatchProblem;
+
+template <int Field>
+__device__ __forceinline__ int find_problem(const BatchProblem *pr, int count, int x) {
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    const int b = Field == 0 ? pr[mid].rowblk_begin
+                  : Field == 1 ? pr[mid].colblk_begin
+                  : Field == 2 ? pr[mid].digA_begin
+                  : Field == 3 ? pr[mid].digB_begin
+                               : pr[mid].out_begin;
+    if (b <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void absmax_rows_b(const BatchProblem *__restrict__ pr, int count,
+                              unsigned long long *bits) {
+  const int q = find_problem<0>(pr, count, blockIdx.y);
+  const BatchProblem &b = pr[q];
+  if ((int)blockIdx.x * 32 >= b.k) return;
+  mdgi::absmax_block(b.p, b.m, b.k, b.A, b.lda, bits + b.offE, nullptr, blockIdx.x,
+                     blockIdx.y - b.rowblk_begin);
+}
+
+__global__ void absmax_cols_b(const BatchProblem *__restrict__ pr, int count,
+                              unsigned long long *bits) {
+  const int q = find_problem<1>(pr, count, blockIdx.y);
+  const BatchProblem &b = pr[q];
+  if ((int)blockIdx.x * 32 >= b.n) return;
+  mdgi::absmax_block(b.p, b.k, b.n, b.B, b.ldb, nullptr, bits + b.offF, blockIdx.x,
+                     blockIdx.y - b.colblk_begin);
+}
+
+__global__ void exps_b(int count, const unsigned long long *__restrict__ bits, int *__restrict__ E) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) E[i] = mdgi::scale_exp(__longlong_as_double((long long)bits[i]));
+}
+
+template <int NW, int Side>
+__global__ void digits_b(const BatchProblem *__restrict__ pr, int count, const int *__restrict__ E) {
+  const int q = find_problem<Side == 0 ? 2 : 3>(pr, count, blockIdx.x);
+  const BatchProblem &b = pr[q];
+  const int pc = blockIdx.y * blockDim.x + threadIdx.x;
+  if (pc >= b.Kp) return;
+  if (Side == 0)
+    mdgi::digits_elem<NW>(b.p, b.s, b.m, b.k, b.A, b.lda, E + b.offE, 0, b.dA, b.Kp, b.plane_a,
+                          b.Mp, b.Kp, blockIdx.x - b.digA_begin, pc);
+  else
+    mdgi::digits_elem<NW>(b.p, b.s, b.n, b.k, b.B, b.ldb, E + b.offF, 1, b.dB, b.Kp, b.plane_b,
+                          b.Np, b.Kp, blockIdx.x - b.digB_begin, pc);
+}
+
+template <int NW>
+__global__ void __launch_bounds__(128) renorm_b(const BatchProblem *__restrict__ pr, int count,
+                                                const int *__restrict__ E) {
+  const int q = find_problem<4>(pr, count, blockIdx.x);
+  const BatchProblem &b = pr[q];
+  const int r = blockIdx.x - b.out_begin, c = blockIdx.y * blockDim.x + threadIdx.x;
+  const int KB = b.Kp / 64;
+  switch (b.p) {
+    case 2:
+      mdgi::renorm_elems<2, NW, 1>(b.s, b.D, KB, b.m, b.n, b.chunks, b.plane_c, b.Np,
+                                   E + b.offE, E + b.offF, b.C, b.ldc, r, c);
+      break;
+    case 4:
+      mdgi::renorm_elems<4, NW, 1>(b.s, b.D, KB, b.m, b.n, b.chunks, b.plane_c, b.Np,
+                                   E + b.offE, E + b.offF, b.C, b.ldc, r, c);
+      break;
+    case 8:
+      mdgi::renorm_elems<8, NW, 1>(b.s, b.D, KB, b.m, b.n, b.chunks, b.plane_c, b.Np,
+                                   E + b.offE, E + b.offF, b.C, b.ldc, r, c);
+      break;
+    default:
+      mdgi::renorm_elems<16, NW, 1>(b.s, b.D, KB, b.m, b.n, b.chunks, b.plane_c, b.Np,
+                                    E + b.offE, E + b.offF, b.C, b.ldc, r, c);
+      break;
+  }
+}
+
+struct Layout {
+  size_t off_probs, off_groups, off_bits, off_exps, total;
+  std::vector<size_t> off_dA, off_dB, off_chunks;
+};
+
+// Sizes and offsets; fills the host tables when `ws` is non-null.
+int plan_batch(const mdg_problem *problems, int count, Layout *L, mdg_batch_s *h,
+               std::vector<BatchProblem> *hp, std::vector<mdgi::GroupedProblem> *hg, char *ws) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = mdgi::align_up(off + bytes, 256);
+    return o;
+  };
+  L->off_probs = take(sizeof(BatchProblem) * count);
+  L->off_groups = take(sizeof(mdgi::GroupedProblem) * count);
+  int rows = 0, cols = 0;
+  for (int i = 0; i < count; ++i) {
+    rows += std::max(problems[i].m, 1);
+    cols += std::max(problems[i].n, 1);
+  }
+  L->off_bits = take(sizeof(unsigned long long) * (size_t)(rows + cols));
+  L->off_exps = take(sizeof(int) * (size_t)(rows + cols));
+  L->off_dA.resize(count);
+  L->off_dB.resize(count);
+  L->off_chunks.resize(count);
+  int rowblk = 0, colblk = 0, digA = 0, digB = 0, outr = 0, tiles = 0, offE = 0, offF = rows;
+  h->nw = 4;
+  for (int i = 0; i < count; ++i) {
+    const mdg_problem &q = problems[i];
+    const int s = mdg_default_slices(q.p), D = s;
+    const int Mp = (int)mdgi::align_up(std::max(q.m, 1), 128);
+    const int Np = (int)mdgi::align_up(std::max(q.n, 1), 256);
+    const int Kp = (int)mdgi::align_up(std::max(q.k, 1), 64);
+    const int nch = mdgi::total_chunks(s, D, Kp / 64);
+    L->off_dA[i] = take(sizeof(__nv_bfloat16) * (size_t)s * Mp * Kp);
+    L->off_dB[i] = take(sizeof(__nv_bfloat16) * (size_t)s * Np * Kp);
+    L->off_chunks[i] = take(sizeof(int) * (size_t)nch * Mp * Np);
+    const int nw = std::max(mdgi::words_for(s, 1), mdgi::words_for(1, D));
+    if (!nw) return MDG_ERROR_NOT_SUPPORTED;
+    h->nw = std::max(h->nw, nw);
+    if (ws) {
+      BatchProblem b{};
+      b.p = q.p; b.s = s; b.D = D; b.m = q.m; b.n = q.n; b.k = q.k;
+      b.Mp = Mp; b.Np = Np; b.Kp = Kp;
+      b.A = q.A; b.B = q.B; b.C = q.C; b.lda = q.lda; b.ldb = q.ldb; b.ldc = q.ldc;
+      b.offE = offE; b.offF = offF;
+      b.dA = reinterpret_cast<__nv_bfloat16 *>(ws + L->off_dA[i]);
+      b.dB = reinterpret_cast<__nv_bfloat16 *>(ws + L->off_dB[i]);
+      b.chunks = reinterpret_cast<int *>(ws + L->off_chunks[i]);
+      b.plane_a = (long long)Mp * Kp;
+      b.plane_b = (long long)Np * Kp;
+      b.plane_c = (long long)Mp * Np;
+      b.rowblk_begin = rowblk; b.colblk_begin = colblk;
+      b.digA_begin = digA; b.digB_begin = digB; b.out_begin = outr;
+      hp->push_back(b);
+      mdgi::GroupedProblem g{};
+      MDG_TRY(mdgi::encode_plane_map(g.tmA, b.dA, Kp, (long long)s * Mp, 128));
+      MDG_TRY(mdgi::encode_plane_map(g.tmB, b.dB, Kp, (long long)s * Np, 256));
+      g.s = s; g.D = D; g.Mp = Mp; g.Np = Np; g.KB = Kp / 64; g.tile_begin = tiles;
+      g.out = b.chunks;
+      g.plane_c = b.plane_c;
+      hg->push_back(g);
+    }
+    rowblk += (std::max(q.m, 1) + 255) / 256;
+    colblk += (std::max(q.k, 1) + 255) / 256;
+    digA += Mp;
+    digB += Np;
+    outr += std::max(q.m, 1);
+    tiles += (Mp / 128) * (Np / 256);
+    offE += std::max(q.m, 1);
+    offF += std::max(q.n, 1);
+    h->max_k = std::max(h->max_k, q.k);
+    h->max_n = std::max(h->max_n, q.n);
+    h->max_Kp = std::max(h->max_Kp, Kp);
+  }
+  h->count = count;
+  h->total_rowblk = rowblk;
+  h->total_colblk = colblk;
+  h->total_digA = digA;
+  h->total_digB = digB;
+  h->total_out = outr;
+  h->total_tiles = tiles;
+  h->total_exps = rows + cols;
+  L->total = off;
+  return MDG_SUCCESS;
+}
+
+int check_problems(const mdg_problem *problems, int count) {
+  if (count < 0) return MDG_ERROR_INVALID_SIZE;
+  if (count > 0 && !problems) return MDG_ERROR_NULL_POINTER;
+  for (int i = 0; i < count; ++i) {
+    const mdg_problem &q = problems[i];
+    if (!mdgi::valid_p(q.p)) return MDG_ERROR_INVALID_LIMBS;
+    if (q.m <= 0 || q.n <= 0 || q.k <= 0) return MDG_ERROR_INVALID_SIZE;
+    if (q.lda < q.k || q.ldb < q.n || q.ldc < q.n) return MDG_ERROR_INVALID_SIZE;
+    if (!q.A || !q.B || !q.C) return MDG_ERROR_NULL_POINTER;
+  }
+  return MDG_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t mdg_batch_workspace_size(const mdg_problem *problems, int count) {
+  if (check_problems(problems, count) != MDG_SUCCESS || count == 0) return 0;
+  Layout L;
+  mdg_batch_s h;
+  if (plan_batch(problems, count, &L, &h, nullptr, nullptr, nullptr) != MDG_SUCCESS) return 0;
+  return L.total;
+}
+
+int mdg_batch_create(const mdg_problem *problems, int count, void *workspace,
+                     size_t workspace_bytes, void *stream, mdg_batch_s **out) {
+  if (!out) return MDG_ERROR_NULL_POINTER;
+  *out = nullptr;
+  MDG_TRY(check_problems(problems, count));
+  if (count == 0) return MDG_ERROR_INVALID_SIZE;
+  Layout L;
+  mdg_batch_s probe;
+  MDG_TRY(plan_batch(problems, count, &L, &probe, nullptr, nullptr, nullptr));
+  if (!workspace || workspace_bytes < L.total) return MDG_ERROR_WORKSPACE;
+  char *ws = reinterpret_cast<char *>(workspace);
+  auto *h = new mdg_batch_s();
+  std::vector<BatchProblem> hp;
+  std::vector<mdgi::GroupedProblem> hg;
+  int st = plan_batch(problems, count, &L, h, &hp, &hg, ws);
+  if (st != MDG_SUCCESS) {
+    delete h;
+    return st;
+  }
+  h->dprobs = reinterpret_cast<BatchProblem *>(ws + L.off_probs);
+  h->dgroups = reinterpret_cast<mdgi::GroupedProblem *>(ws + L.off_groups);
+  h->bits = reinterpret_cast<unsigned long long *>(ws + L.off_bits);
+  h->exps = reinterpret_cast<int *>(ws + L.off_exps);
+  cudaStream_t s = mdgi::as_stream(stream);
+  cudaError_t e = cudaMemcpyAsync(h->dprobs, hp.data(), sizeof(BatchProblem) * count,
+                                  cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->dgroups, hg.data(), sizeof(mdgi::GroupedProblem) * count,
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    mdgi::set_cuda_error(e);
+    delete h;
+    return MDG_ERROR_CUDA;
+  }
+  *out = h;
+  return MDG_SUCCESS;
+}
+
+int mdg_batch_run(mdg_batch_s *h, void *stream) {
+  if (!h) return MDG_ERROR_NULL_POINTER;
+  cudaStream_t st = mdgi::as_stream(stream);
+  MDG_TRY_CUDA(cudaMemsetAsync(h->bits, 0, sizeof(unsigned long long) * h->total_exps, st));
+  absmax_rows_b<<<dim3(mdgi::ceil_div(h->max_k, 32), h->total_rowblk), dim3(32, 8), 0, st>>>(
+      h->dprobs, h->count, h->bits);
+  MDG_TRY_LAUNCH();
+  absmax_cols_b<<<dim3(mdgi::ceil_div(h->max_n, 32), h->total_colblk), dim3(32, 8), 0, st>>>(
+      h->dprobs, h->count, h->bits);
+  MDG_TRY_LAUNCH();
+  exps_b<<<mdgi::ceil_div(h->total_exps, 256), 256, 0, st>>>(h->total_exps, h->bits, h->exps);
+  MDG_TRY_LAUNCH();
+  const dim3 ga(h->total_digA, mdgi::ceil_div(h->max_Kp, 128));
+  const dim3 gb(h->total_digB, mdgi::ceil_div(h->max_Kp, 128));
+  const dim3 gr(h->total_out, mdgi::ceil_div(h->max_n, 128));
+#define MDG_BATCH_NW(W)                                                            \
+  digits_b<W, 0><<<ga, 128, 0, st>>>(h->dprobs, h->count, h->exps);                \
+  MDG_TRY_LAUNCH();                                                                \
+  digits_b<W, 1><<<gb, 128, 0, st>>>(h->dprobs, h->count, h->exps);                \
+  MDG_TRY_LAUNCH();                                                                \
+  MDG_TRY(mdgi::launch_diag_gemm_grouped(h->dgroups, h->count, h->total_tiles, st)); \
+  renorm_b<W><<<gr, 128, 0, st>>>(h->dprobs, h->count, h->exps);                   \
+  MDG_TRY_LAUNCH();
+  switch (h->nw) {
+    case 4: MDG_BATCH_NW(4); break;
+    case 6: MDG_BATCH_NW(6); break;
+    case 10: MDG_BATCH_NW(10); break;
+    default: MDG_BATCH_NW(16); break;
+  }
+#undef MDG_BATCH_NW
+  return MDG_SUCCESS;
+}
+
+void mdg_batch_destroy(mdg_batch_s *h) { delete h; }
+
+}  // extern "C"

@@ -260,6 +260,12 @@ size_t mdg_gemm_batched_workspace_size(int form, const mdg_problem *problems, in
   size_t total = align_up(sizeof(mdg_problem) * (size_t)count, 256) +
                  align_up(sizeof(int) * (size_t)(count + 1), 256);
   if (form == MDG_FORM_PLAIN) return total;
+  if (form == MDG_FORM_SLICE_BF16) {
+    std::vector<mdg_problem> live;
+    for (int i = 0; i < count; ++i)
+      if (problems[i].m > 0 && problems[i].n > 0 && problems[i].k > 0) live.push_back(problems[i]);
+    return live.empty() ? 0 : mdg_batch_workspace_size(live.data(), (int)live.size());
+  }
   size_t mx = 0;
   for (int i = 0; i < count; ++i) {
     const mdg_problem &q = problems[i];
@@ -307,8 +313,28 @@ int mdg_gemm_batched(int form, const mdg_problem *problems, int count, const mdg
     MDG_TRY_CUDA(cudaStreamSynchronize(st));
     return launch_plain_batched(dprobs, count, max_p, dstarts, starts[count], st);
   }
-  // split forms: the stages of each problem in turn on one stream, sharing
-  // the largest workspace
+  if (form == MDG_FORM_SLICE_BF16) {
+    // empty problems: nothing (m or n = 0) or C = 0 (k = 0); the plan takes the rest
+    std::vector<mdg_problem> live;
+    for (int i = 0; i < count; ++i) {
+      const mdg_problem &q = problems[i];
+      if (q.m == 0 || q.n == 0) continue;
+      if (q.k == 0) {
+        MDG_TRY_CUDA(cudaMemset2DAsync(q.C, sizeof(double) * q.ldc * q.p, 0,
+                                       sizeof(double) * q.n * q.p, q.m, st));
+        continue;
+      }
+      live.push_back(q);
+    }
+    if (live.empty()) return MDG_SUCCESS;
+    mdg_batch b = nullptr;
+    MDG_TRY(mdg_batch_create(live.data(), (int)live.size(), workspace, wsb, stream, &b));
+    const int st2 = mdg_batch_run(b, stream);
+    mdg_batch_destroy(b);
+    return st2;
+  }
+  // FP64 split form: the stages of each problem in turn on one stream,
+  // sharing the largest workspace
   void *ws = base + align_up(sizeof(mdg_problem) * (size_t)count, 256) +
              align_up(sizeof(int) * (size_t)(count + 1), 256);
   const size_t wsz = need - (static_cast<char *>(ws) - base);

@@ -197,10 +197,30 @@ __device__ __forceinline__ void drain128(uint32_t taddr, int (&acc)[128]) {
   add_exact(acc + 96, rb);
 }
 
-__global__ void __launch_bounds__(THREADS, 1)
-    diag_gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA,
-                        const __grid_constant__ CUtensorMap tmB, int s, int D, int Mp, int Np,
-                        int KB, int *__restrict__ out, long long plane_c) {
+// One tile of work: where its operands and output live and which of its
+// problem's rows / columns it covers.
+struct TileJob {
+  const CUtensorMap *tmA, *tmB;
+  int s, D, Mp, Np, KB, row, col;
+  int *out;
+  long long plane_c;
+};
+
+// A single problem cut into 128 x 256 tiles.
+struct SingleJobs {
+  const CUtensorMap *tmA, *tmB;
+  int s, D, Mp, Np, KB;
+  int *out;
+  long long plane_c;
+  __device__ int tiles() const { return (Mp / TM) * (Np / TN); }
+  __device__ TileJob job(int t) const {
+    const int MB = Mp / TM;
+    return TileJob{tmA, tmB, s, D, Mp, Np, KB, (t % MB) * TM, (t / MB) * TN, out, plane_c};
+  }
+};
+
+template <class Jobs>
+__device__ __forceinline__ void tc1_body(const Jobs &jobs) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -242,8 +262,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   fence_after();
   const uint32_t tmem_base = *tmem_holder;
 
-  const int MB = Mp / TM;
-  const int tiles = MB * (Np / TN);
+  const int tiles = jobs.tiles();
 
   if (warp == 0) {
     if (lane == 0) {
@@ -254,8 +273,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       bool issued[STAGES];
       for (int i = 0; i < STAGES; ++i) issued[i] = false;
       for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const int row = (tile % MB) * TM, col = (tile / MB) * TN;
-        for (int d = 0; d < D; ++d) {
+        const TileJob jb = jobs.job(tile);
+        const int s = jb.s, KB = jb.KB;
+        for (int d = 0; d < jb.D; ++d) {
           const int ilo = d - (s - 1) > 0 ? d - (s - 1) : 0;
           const int S = mdgi::diag_pairs(d, s) * KB;
           for (int t = 0; t < S; ++t) {
@@ -263,8 +283,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (!mbar_wait(empty(st), ph ^ 1, abort_flag)) goto producer_done;
             mbar_expect_tx(full(st), STAGE_BYTES);
             const uint32_t a_dst = smem_base + st * STAGE_BYTES;
-            tma_load_2d(a_dst, &tmA, kb * TK, i * Mp + row, full(st));
-            tma_load_2d(a_dst + A_BYTES, &tmB, kb * TK, j * Np + col, full(st));
+            tma_load_2d(a_dst, jb.tmA, kb * TK, i * jb.Mp + jb.row, full(st));
+            tma_load_2d(a_dst + A_BYTES, jb.tmB, kb * TK, j * jb.Np + jb.col, full(st));
             last_par[st] = ph;
             issued[st] = true;
             if (++st == STAGES) {
@@ -286,8 +306,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t ph = 0, aph[2] = {0, 0};
       bool any = false;
       for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        for (int d = 0; d < D; ++d) {
-          const int S = mdgi::diag_pairs(d, s) * KB;
+        const TileJob jb = jobs.job(tile);
+        for (int d = 0; d < jb.D; ++d) {
+          const int S = mdgi::diag_pairs(d, jb.s) * jb.KB;
           for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
             if (!mbar_wait(accempty(buf), aph[buf] ^ 1, abort_flag)) goto mma_done;
             fence_after();
@@ -329,11 +350,12 @@ __global__ void __launch_bounds__(THREADS, 1)
     int buf = 0;
     uint32_t aph[2] = {0, 0};
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-      const int row = (tile % MB) * TM + 32 * q + lane;
-      const int col = (tile / MB) * TN + 128 * h;
+      const TileJob jb = jobs.job(tile);
+      const int row = jb.row + 32 * q + lane;
+      const int col = jb.col + 128 * h;
       int chunk = 0;
-      for (int d = 0; d < D; ++d) {
-        const int S = mdgi::diag_pairs(d, s) * KB;
+      for (int d = 0; d < jb.D; ++d) {
+        const int S = mdgi::diag_pairs(d, jb.s) * jb.KB;
         for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
           // lane 0 waits; the verdict is broadcast so the warp stays
           // converged for the .sync.aligned TMEM loads
@@ -351,8 +373,8 @@ __global__ void __launch_bounds__(THREADS, 1)
           buf ^= 1;
           const int g1 = g0 + mdgi::GROUP_STEPS;
           if (g1 % mdgi::CHUNK_STEPS == 0 || g1 >= S) {
-            int4 *dst = reinterpret_cast<int4 *>(out + (size_t)chunk * plane_c +
-                                                 (size_t)row * Np + col);
+            int4 *dst = reinterpret_cast<int4 *>(jb.out + (size_t)chunk * jb.plane_c +
+                                                 (size_t)row * jb.Np + col);
 #pragma unroll
             for (int v = 0; v < 32; ++v) {
               dst[v] = make_int4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
@@ -374,6 +396,40 @@ __global__ void __launch_bounds__(THREADS, 1)
                  "r"(TMEM_COLS)
                  : "memory");
   if (threadIdx.x == 0 && *abort_flag) atomicExch(&g_tc_error, 1);
+}
+
+
+__global__ void __launch_bounds__(THREADS, 1)
+    diag_gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA,
+                        const __grid_constant__ CUtensorMap tmB, int s, int D, int Mp, int Np,
+                        int KB, int *__restrict__ out, long long plane_c) {
+  tc1_body(SingleJobs{&tmA, &tmB, s, D, Mp, Np, KB, out, plane_c});
+}
+
+// Many problems: a table of GroupedProblem in global memory (tensor maps
+// included, 64-byte aligned), tiles numbered problem after problem.
+struct GroupedJobs {
+  const mdgi::GroupedProblem *probs;
+  int count, total;
+  __device__ int tiles() const { return total; }
+  __device__ TileJob job(int t) const {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (probs[mid].tile_begin <= t) lo = mid; else hi = mid - 1;
+    }
+    const mdgi::GroupedProblem &g = probs[lo];
+    const int lt = t - g.tile_begin, MB = g.Mp / TM;
+    return TileJob{reinterpret_cast<const CUtensorMap *>(g.tmA),
+                   reinterpret_cast<const CUtensorMap *>(g.tmB), g.s, g.D, g.Mp, g.Np, g.KB, (lt % MB) * TM, (lt / MB) * TN,
+                   g.out, g.plane_c};
+  }
+};
+
+__global__ void __launch_bounds__(THREADS, 1)
+    diag_gemm_tc_grouped_kernel(const mdgi::GroupedProblem *__restrict__ probs, int count,
+                                int total) {
+  tc1_body(GroupedJobs{probs, count, total});
 }
 
 // ------------------------------------------------------------------------
@@ -700,6 +756,28 @@ int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, co
     diag_gemm_tc_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(ma, mb, s, D, Mp, Np, Kp / TK, chunks,
                                                            plane_c);
   }
+  MDG_TRY_LAUNCH();
+  return MDG_SUCCESS;
+}
+
+int encode_plane_map(void *map128, const void *base, int Kp, long long rows_total, int box_rows) {
+  return make_map(reinterpret_cast<CUtensorMap *>(map128), base, Kp, rows_total, box_rows);
+}
+
+int launch_diag_gemm_grouped(const GroupedProblem *dev_probs, int count, int total_tiles,
+                             cudaStream_t st) {
+  if (total_tiles == 0) return MDG_SUCCESS;
+  static int configured_dev = -1;
+  int dev = 0, sms = 0;
+  MDG_TRY_CUDA(cudaGetDevice(&dev));
+  if (configured_dev != dev) {
+    MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc_grouped_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    configured_dev = dev;
+  }
+  MDG_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = total_tiles < sms ? total_tiles : sms;
+  diag_gemm_tc_grouped_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(dev_probs, count, total_tiles);
   MDG_TRY_LAUNCH();
   return MDG_SUCCESS;
 }

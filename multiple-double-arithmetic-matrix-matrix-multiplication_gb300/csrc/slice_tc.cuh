@@ -60,6 +60,20 @@ int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, co
 int launch_renorm(int p, int s, int D, int KB, int m, int n, const int *chunks,
                   long long plane_c, int ldcd, const int *E, const int *F, double *C, int ldc,
                   cudaStream_t st);
+// One problem of a grouped diagonal GEMM (single-CTA tcgen05 kernel,
+// 128 x 256 tiles): tensor maps of its digit planes, sizes, first global
+// tile, output chunk planes.  Lives in global memory, 64-byte aligned.
+struct alignas(64) GroupedProblem {
+  unsigned char tmA[128];  // CUtensorMap, A planes, box 64 x 128
+  unsigned char tmB[128];  // CUtensorMap, B planes, box 64 x 256
+  int s, D, Mp, Np, KB, tile_begin;
+  int *out;
+  long long plane_c;
+};
+int encode_plane_map(void *map128, const void *base, int Kp, long long rows_total, int box_rows);
+int launch_diag_gemm_grouped(const GroupedProblem *dev_probs, int count, int total_tiles,
+                             cudaStream_t st);
+
 // Waits for the device; MDG_ERROR_TIMEOUT if a bounded wait of the tcgen05
 // engine gave up since the last call (the flag is then cleared).
 int tc_device_status();

@@ -305,3 +305,54 @@ def test_zero_k_gives_zero(api):
         C = api.gemm(A, B, form, out=torch.full((5, 6, 4), 3.0, dtype=torch.float64,
                                                  device="cuda"))
         assert torch.all(C == 0)
+
+
+# -------------------------------------------------------------- batched --
+
+def _batch_case(inputs, count, seed, shrink):
+    probs, rng = inputs.batched_problems(count, seed=seed)
+    probs = [(P, max(1, m // shrink), max(1, n // shrink), max(1, k // shrink))
+             for P, m, n, k in probs]
+    return probs, inputs.batched_operands(probs, rng)
+
+
+def test_batched_slice_equals_single_problem_results(api, inputs):
+    """One grouped launch per stage over mixed P and uneven sizes gives,
+    for every problem, the bits of the single-problem BF16 GEMM."""
+    probs, ops = _batch_case(inputs, 24, 11, 2)
+    probs.append((4, 3, 5, 0))          # k = 0: C = 0
+    ops.append((np.zeros((3, 0, 4)), np.zeros((0, 5, 4))))
+    dev_ops = [(dev(A), dev(B)) for A, B in ops]
+    Cs = api.gemm_batched(dev_ops, "slice_bf16")
+    for (A, B), C in zip(dev_ops, Cs):
+        if A.shape[1] == 0:
+            assert torch.all(C == 0)
+        else:
+            assert torch.equal(C, api.gemm(A, B, "slice_bf16"))
+
+
+def test_batched_plan_graph_capture(api, orc, inputs):
+    """The plan's run() captured in a CUDA graph and replayed; results are
+    the oracle's bits (checked on three problems)."""
+    probs, ops = _batch_case(inputs, 16, 12, 4)
+    dev_ops = [(dev(A), dev(B)) for A, B in ops]
+    plan = api.BatchPlan(dev_ops)
+    plan.run()
+    torch.cuda.synchronize()
+    first = [C.clone() for C in plan.Cs]
+    for C in plan.Cs:
+        C.fill_(np.nan)
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            plan.run(stream=s)
+    g.replay()
+    g.replay()
+    torch.cuda.synchronize()
+    for a, b in zip(first, plan.Cs):
+        assert torch.equal(a, b)
+    for (P, m, n, k), (A, B), C in list(zip(probs, ops, plan.Cs))[:3]:
+        sl = api.default_slices(P)
+        assert np.array_equal(host(C), orc.gemm_slices(P, sl, sl, A, B, m, n, k))
