@@ -216,6 +216,50 @@ def event_time(fn, stream, iters=1):
     return e0.elapsed_time(e1) / 1e3 / iters
 
 
+def bench_batched(api, inputs, stream):
+    """The batched workload (256 problems, m, n, k in {32..512}, P in {2, 4, 8},
+    seed 3): the BF16 slice-digit plan replayed as one CUDA graph, against a
+    loop of per-problem plain launches and the one-launch plain batch."""
+    import torch
+    probs, rng = inputs.batched_problems(256, seed=3)
+    ops = inputs.batched_operands(probs, rng)
+    dev_ops = [(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()) for A, B in ops]
+    flops = sum(2.0 * m * n * k for _, m, n, k in probs)
+    plan = api.BatchPlan(dev_ops)
+    plan.run()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            plan.run(stream=s)
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    t_graph = event_time(g.replay, torch.cuda.current_stream(), iters=5)
+    # every C of the graph equals the single-problem slice GEMM
+    same = all(torch.equal(C, api.gemm(A, B, "slice_bf16")) for (A, B), C in
+               list(zip(dev_ops, plan.Cs))[:16])
+    outs = [torch.empty((A.shape[0], B.shape[1], A.shape[2]), dtype=torch.float64,
+                        device="cuda") for A, B in dev_ops]
+
+    def plain_loop():
+        for (A, B), C in zip(dev_ops, outs):
+            api.gemm(A, B, "plain", out=C)
+
+    t_loop = event_time(plain_loop, stream, iters=1)
+    api.gemm_batched(dev_ops, "plain")
+    t_pb = event_time(lambda: api.gemm_batched(dev_ops, "plain"), stream, iters=1)
+    return {"workload": "256 problems, m,n,k ~ U{32..512 step 32}, P ~ U{2,4,8}, seed 3",
+            "md_gflop": flops / 1e9,
+            "slice_graph_gflops": flops / t_graph / 1e9, "slice_graph_ms": t_graph * 1e3,
+            "slice_launches_per_batch": 8,
+            "plain_loop_gflops": flops / t_loop / 1e9, "plain_loop_ms": t_loop * 1e3,
+            "plain_batched_gflops": flops / t_pb / 1e9, "plain_batched_ms": t_pb * 1e3,
+            "slice_equals_single_problem": bool(same)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -340,6 +384,10 @@ def main():
         if "fp64split" in forms:
             forms["slice_over_fp64split"] = forms["slice_bf16"]["gflops"] / forms["fp64split"]["gflops"]
 
+    batched = None
+    if not args.no_forms and rank == 0:
+        batched = bench_batched(api, inputs, stream)
+
     cpu = None
     if not args.no_cpu and rank == 0:
         v, sample, _ = cpu_sample(P, A, B, 6.0, os.cpu_count() or 1)
@@ -370,6 +418,7 @@ def main():
                            "sample": f"{len(rows)}x{len(cols)} entries, exact integer product"},
             "cpu_baseline": cpu,
             "forms": forms,
+            "batched": batched,
         }
         print(json.dumps(line))
 

@@ -248,6 +248,16 @@ def test_slice_gemm_bit_exact_against_oracle(api, orc, inputs, engine, P, shape,
     assert np.array_equal(got, orc.gemm_slices(P, s, s, A, B, m, n, k))
 
 
+def test_slice_gemm_hexa_double_bit_exact(api, orc, inputs):
+    """P = 16 through the BF16 form (108 digits, 5886 digit pairs)."""
+    rng = np.random.default_rng(16)
+    m, n, k = 9, 7, 20
+    A = inputs.uniform_pd(rng, (m, k), 16)
+    B = inputs.uniform_pd(rng, (k, n), 16)
+    got = host(api.gemm(dev(A), dev(B), "slice_bf16"))
+    assert np.array_equal(got, orc.gemm_slices(16, 108, 108, A, B, m, n, k))
+
+
 @pytest.mark.parametrize("name", ["dd64", "qd1024", "od2048_spread"])
 def test_slice_error_bits_not_worse_than_plain(api, orc, inputs, name):
     import oracle.exact as ex
