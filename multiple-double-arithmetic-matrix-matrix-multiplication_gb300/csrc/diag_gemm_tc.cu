@@ -23,6 +23,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstdlib>
 
 #include "common.cuh"
@@ -506,7 +507,7 @@ __device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
     diag_gemm_tc2_kernel(const __grid_constant__ CUtensorMap tmA,
                          const __grid_constant__ CUtensorMap tmB, int s, int D, int Mp, int Np,
-                         int KB, int *__restrict__ out, long long plane_c) {
+                         int KB, int *__restrict__ out, long long plane_c, int parts) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -552,7 +553,29 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
 
   const int MB = Mp / 256;
   const int tiles = MB * (Np / TN2);
+  const int units = tiles * parts;
   const int cid = blockIdx.x >> 1, ncl = gridDim.x >> 1;
+  // a unit is one part of one tile: the diagonals [d0, d1) whose digit-pair
+  // counts add up to about 1/parts of the tile's work
+  auto unit_range = [&](int u, int &tile, int &d0, int &d1) {
+    tile = u % tiles;
+    const int part = u / tiles;
+    int total = 0;
+    for (int d = 0; d < D; ++d) total += mdgi::diag_pairs(d, s);
+    const long long lo = (long long)total * part / parts, hi = (long long)total * (part + 1) / parts;
+    int cum = 0;
+    d0 = D;
+    d1 = D;
+    for (int d = 0; d < D; ++d) {
+      if (cum >= lo && d0 == D) d0 = d;
+      if (cum >= hi) {
+        d1 = d;
+        break;
+      }
+      cum += mdgi::diag_pairs(d, s);
+    }
+    if (d0 > d1) d0 = d1;
+  };
 
   if (warp == 0) {
     if (lane == 0) {
@@ -562,10 +585,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
       uint32_t last_par[STAGES2];
       bool issued[STAGES2];
       for (int i = 0; i < STAGES2; ++i) issued[i] = false;
-      for (int tile = cid; tile < tiles; tile += ncl) {
+      for (int u = cid; u < units; u += ncl) {
+        int tile, d0, d1;
+        unit_range(u, tile, d0, d1);
         const int row = (tile % MB) * 256 + (int)rank * TM;
         const int col = (tile / MB) * TN2 + (int)rank * BH;
-        for (int d = 0; d < D; ++d) {
+        for (int d = d0; d < d1; ++d) {
           const int ilo = d - (s - 1) > 0 ? d - (s - 1) : 0;
           const int S = mdgi::diag_pairs(d, s) * KB;
           for (int t = 0; t < S; ++t) {
@@ -596,8 +621,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
       int st = 0, buf = 0;
       uint32_t ph = 0, aph[2] = {0, 0};
       bool any = false;
-      for (int tile = cid; tile < tiles; tile += ncl) {
-        for (int d = 0; d < D; ++d) {
+      for (int u = cid; u < units; u += ncl) {
+        int tile, d0, d1;
+        unit_range(u, tile, d0, d1);
+        for (int d = d0; d < d1; ++d) {
           const int S = mdgi::diag_pairs(d, s) * KB;
           for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
             if (!mbar_wait(accempty(buf), aph[buf] ^ 1, abort_flag)) goto mma_done;
@@ -640,11 +667,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
     int buf = 0;
     uint32_t aph[2] = {0, 0};
     const uint32_t accempty0[2] = {map_to_rank0(accempty(0)), map_to_rank0(accempty(1))};
-    for (int tile = cid; tile < tiles; tile += ncl) {
+    for (int u = cid; u < units; u += ncl) {
+      int tile, d0, d1;
+      unit_range(u, tile, d0, d1);
       const int row = (tile % MB) * 256 + (int)rank * TM + 32 * q + lane;
       const int col = (tile / MB) * TN2 + 128 * h;
       int chunk = 0;
-      for (int d = 0; d < D; ++d) {
+      for (int d = 0; d < d0; ++d) chunk += mdgi::diag_chunks(d, s, KB);
+      for (int d = d0; d < d1; ++d) {
         const int S = mdgi::diag_pairs(d, s) * KB;
         for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
           int ok = 1;
@@ -747,9 +777,26 @@ int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, co
   MDG_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   if (pair) {
     const int tiles = (Mp / 256) * (Np / TN2);
-    const int clusters = tiles < sms / 2 ? tiles : sms / 2;
-    diag_gemm_tc2_kernel<<<2 * clusters, THREADS, SMEM2_BYTES, st>>>(ma, mb, s, D, Mp, Np,
-                                                                      Kp / TK, chunks, plane_c);
+    // split tiles into `parts` diagonal ranges when that shrinks the idle
+    // part of the last wave of clusters
+    const int ncl = sms / 2;
+    int parts = 1;
+    double best = 2.0;
+    for (int u = 1; u <= 8 && u <= D; ++u) {
+      const long long units = (long long)tiles * u;
+      const long long waves = (units + ncl - 1) / ncl;
+      const double waste = (double)(waves * ncl - units) / (double)(waves * ncl);
+      if (waste < best - 0.01) {
+        best = waste;
+        parts = u;
+      }
+    }
+    const char *pe = std::getenv("MDG_TC_PARTS");
+    if (pe && *pe) parts = std::max(1, std::min(8, std::atoi(pe)));
+    const long long units = (long long)tiles * parts;
+    const int clusters = units < ncl ? (int)units : ncl;
+    diag_gemm_tc2_kernel<<<2 * clusters, THREADS, SMEM2_BYTES, st>>>(
+        ma, mb, s, D, Mp, Np, Kp / TK, chunks, plane_c, parts);
   } else {
     const int tiles = (Mp / TM) * (Np / TN);
     const int grid = tiles < sms ? tiles : sms;

@@ -30,17 +30,27 @@ __device__ __forceinline__ void wide_add_shifted(uint64_t (&w)[NW], int64_t v, i
 }
 
 // The 64 bits of w starting at bit pos (0 <= pos < 64 NW); bits above the
-// top word read as the sign.
+// top word read as the sign.  The word offset is applied as a barrel shift
+// (one predicated shift per bit of the offset) so that every access has a
+// compile-time index and w stays in registers.
 template <int NW>
 __device__ __forceinline__ uint64_t wide_bits64(const uint64_t (&w)[NW], int pos) {
   const int qw = pos >> 6, r = pos & 63;
   const uint64_t fill = (uint64_t)((int64_t)w[NW - 1] >> 63);
-  uint64_t lo = fill, hi = fill;
+  uint64_t t[NW + 1];
 #pragma unroll
-  for (int i = 0; i < NW; ++i) {
-    if (i == qw) lo = w[i];
-    if (i == qw + 1) hi = w[i];
+  for (int i = 0; i < NW; ++i) t[i] = w[i];
+  t[NW] = fill;
+#pragma unroll
+  for (int bit = 1; bit <= NW; bit <<= 1) {
+    const bool on = (qw & bit) != 0;
+#pragma unroll
+    for (int i = 0; i <= NW; ++i) {
+      const uint64_t src = (i + bit <= NW) ? t[i + bit] : fill;
+      t[i] = on ? src : t[i];
+    }
   }
+  const uint64_t lo = t[0], hi = NW >= 1 ? t[1] : fill;
   return r ? ((lo >> r) | (hi << (64 - r))) : lo;
 }
 
@@ -54,15 +64,18 @@ __device__ __forceinline__ int wide_msb(const uint64_t (&w)[NW]) {
   return t;
 }
 
-// Any bit set strictly below position pos (pos >= 0)?
+// Any bit set strictly below position pos (pos >= 0)?  Masks instead of
+// selects on the word index, for the same reason as wide_bits64.
 template <int NW>
 __device__ __forceinline__ bool wide_any_below(const uint64_t (&w)[NW], int pos) {
   const int qw = pos >> 6, r = pos & 63;
+  const uint64_t low = r ? ((1ull << r) - 1) : 0ull;
   uint64_t acc = 0;
 #pragma unroll
   for (int i = 0; i < NW; ++i) {
-    if (i < qw) acc |= w[i];
-    if (i == qw && r) acc |= w[i] & ((1ull << r) - 1);
+    const uint64_t m_lt = 0ull - (uint64_t)(i < qw);
+    const uint64_t m_eq = 0ull - (uint64_t)(i == qw);
+    acc |= (w[i] & m_lt) | (w[i] & m_eq & low);
   }
   return acc != 0;
 }

@@ -100,6 +100,81 @@ __device__ __forceinline__ void digits_elem(int P, int s, int rows, int cols,
   out[0] = __float2bfloat16_rn((float)top);
 }
 
+// Four consecutive k-positions per thread: the same digits as digits_elem,
+// written as one 8-byte vector (4 BF16) per plane.  pc0 is a multiple of 4;
+// cols_pad, ld_out and plane_stride are multiples of 4.
+template <int NW>
+__device__ __forceinline__ void digits_elem4(int P, int s, int rows, int cols,
+                                             const double *__restrict__ X, int ldx,
+                                             const int *__restrict__ E, int trans,
+                                             __nv_bfloat16 *__restrict__ planes, int ld_out,
+                                             long long plane_stride, int rows_pad, int cols_pad,
+                                             int pr, int pc0) {
+  if (pc0 >= cols_pad || pr >= rows_pad) return;
+  uint2 *out = reinterpret_cast<uint2 *>(planes + (size_t)pr * ld_out + pc0);
+  const long long vstride = plane_stride / 4;
+  if (pr >= rows || pc0 >= cols) {
+    for (int i = 0; i < s; ++i) out[i * vstride] = make_uint2(0, 0);
+    return;
+  }
+  const int S = 7 + 8 * (s - 1);
+  const int Er = E[pr];
+  uint64_t w[4][NW];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+#pragma unroll
+    for (int i = 0; i < NW; ++i) w[e][i] = 0;
+  }
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int pc = pc0 + e;
+    const double *a = trans ? X + ((size_t)pc * ldx + pr) * P : X + ((size_t)pr * ldx + pc) * P;
+    for (int l = 0; l < P; ++l) {
+      const double x = pc < cols ? a[l] : 0.0;
+      if (x == 0.0) continue;
+      int ex;
+      const double f = frexp(x, &ex);
+      const int64_t m = (int64_t)ldexp(f, 53);
+      const int q = ex - 53 + S - Er;
+      if (q >= 0) {
+        mdgi::wide_add_shifted<NW>(w[e], m, q);
+      } else if (q > -64) {
+        mdgi::wide_add_shifted<NW>(w[e], m >> (-q), 0);
+      } else {
+        mdgi::wide_add_shifted<NW>(w[e], m < 0 ? -1 : 0, 0);
+      }
+    }
+  }
+  int carry[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int wi = 0; wi < NW; ++wi) {
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int p = wi * 8 + b;
+      if (p < s - 1) {
+        uint32_t packed[2];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int t = (int)((w[e][wi] >> (8 * b)) & 255) + carry[e];
+          const int d = t >= 128 ? t - 256 : t;
+          carry[e] = t >= 128 ? 1 : 0;
+          const uint32_t bits = __bfloat16_as_ushort(__float2bfloat16_rn((float)d));
+          if (e & 1) packed[e >> 1] |= bits << 16; else packed[e >> 1] = bits;
+        }
+        out[(s - 1 - p) * vstride] = make_uint2(packed[0], packed[1]);
+      }
+    }
+  }
+  uint32_t packed[2];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int top = (int)(int64_t)mdgi::wide_bits64<NW>(w[e], 8 * (s - 1)) + carry[e];
+    const uint32_t bits = __bfloat16_as_ushort(__float2bfloat16_rn((float)top));
+    if (e & 1) packed[e >> 1] |= bits << 16; else packed[e >> 1] = bits;
+  }
+  out[0] = make_uint2(packed[0], packed[1]);
+}
+
 // --------------------------------------------------------------- renorm --
 // W = sum_d C_d 256^(D-1-d) is built bottom-up (Horner from the least
 // significant diagonal): T = C_{D-1}; repeatedly emit the low byte of T as

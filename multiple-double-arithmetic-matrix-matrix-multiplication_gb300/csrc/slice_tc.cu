@@ -57,6 +57,18 @@ __global__ void digits_kernel(int P, int s, int rows, int cols, const double *__
                         rows_pad, cols_pad, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// 4 k-positions per thread, consecutive threads on consecutive positions of
+// one plane row, so plane stores are coalesced for A and B alike.
+template <int NW>
+__global__ void __launch_bounds__(256)
+    digits4_kernel(int P, int s, int rows, int cols, const double *__restrict__ X, int ldx,
+                   const int *__restrict__ E, int trans, __nv_bfloat16 *__restrict__ planes,
+                   int ld_out, long long plane_stride, int rows_pad, int cols_pad) {
+  mdgi::digits_elem4<NW>(P, s, rows, cols, X, ldx, E, trans, planes, ld_out, plane_stride,
+                         rows_pad, cols_pad, blockIdx.y,
+                         (blockIdx.x * blockDim.x + threadIdx.x) * 4);
+}
+
 // ---------------------------------------------------- diagonal GEMM v0 --
 // mma.sync m16n8k16 BF16 -> FP32.  Block 128 x 64, 8 warps as 4 x 2, warp
 // tile 32 x 32 (2 x 4 MMA tiles), K chunk 32 through shared memory.
@@ -270,8 +282,25 @@ int launch_digits(int p, int s, int rows, int cols, const double *X, int ldx, co
   const int NW = words_for(s, 1);
   if (!NW) return MDG_ERROR_NOT_SUPPORTED;
   if (rows_pad == 0 || cols_pad == 0) return MDG_SUCCESS;
-  dim3 grid(ceil_div(cols_pad, 128), rows_pad);
   auto *pl = reinterpret_cast<__nv_bfloat16 *>(planes);
+  const bool vec = (cols_pad % 4 == 0) && (ld_out % 4 == 0) && (plane_stride % 4 == 0) &&
+                   (reinterpret_cast<uintptr_t>(planes) % 8 == 0);
+  if (vec) {
+    const dim3 grid(ceil_div(cols_pad / 4, 256), rows_pad);
+#define MDG_DIGITS8(W)                                                                      \
+  digits4_kernel<W><<<grid, 256, 0, st>>>(p, s, rows, cols, X, ldx, E, trans, pl, ld_out,   \
+                                           plane_stride, rows_pad, cols_pad)
+    switch (NW) {
+      case 4: MDG_DIGITS8(4); break;
+      case 6: MDG_DIGITS8(6); break;
+      case 10: MDG_DIGITS8(10); break;
+      default: MDG_DIGITS8(16); break;
+    }
+#undef MDG_DIGITS8
+    MDG_TRY_LAUNCH();
+    return MDG_SUCCESS;
+  }
+  dim3 grid(ceil_div(cols_pad, 128), rows_pad);
 #define MDG_DIGITS(W)                                                                    \
   digits_kernel<W><<<grid, 128, 0, st>>>(p, s, rows, cols, X, ldx, E, trans, pl, ld_out, \
                                           plane_stride, rows_pad, cols_pad)
