@@ -172,7 +172,7 @@ def run_reference(args):
     kind = "port"
     if oracle.ref_available():
         kind = "reference"
-    vals = []
+    vals, times = [], []
     for i in range(args.warmup + args.steps):
         if kind == "reference":
             # square sub-problem through the reference's matmulqdf, one per thread
@@ -190,11 +190,12 @@ def run_reference(args):
             v, sample, dt = cpu_sample(P, A, B, 3.0, threads)
         if i >= args.warmup:
             vals.append(v)
+            times.append(dt)
     value = float(np.median(vals))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": float(np.median(times)) * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": args.workload},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
@@ -214,6 +215,51 @@ def event_time(fn, stream, iters=1):
     e1.record(stream)
     e1.synchronize()
     return e0.elapsed_time(e1) / 1e3 / iters
+
+
+def pipelined_e2e(api, hA, hB, hC, P, m, n, k, ws_bytes, steps):
+    """Seconds per step of a host-to-host loop with double-buffered device
+    operands: step i computes on one buffer set while the copy streams load
+    step i+1's A and B and return step i-1's C."""
+    import torch
+    comp = torch.cuda.current_stream()
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+    dA = [torch.empty_like(hA, device="cuda") for _ in range(2)]
+    dB = [torch.empty_like(hB, device="cuda") for _ in range(2)]
+    dC = [torch.empty((m, n, P), dtype=torch.float64, device="cuda") for _ in range(2)]
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    ev_in = [torch.cuda.Event() for _ in range(2)]
+    ev_done = [torch.cuda.Event() for _ in range(2)]
+    ev_out = [torch.cuda.Event() for _ in range(2)]
+    for e in ev_done + ev_out:
+        e.record(comp)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(s_in):
+        dA[0].copy_(hA, non_blocking=True)
+        dB[0].copy_(hB, non_blocking=True)
+        ev_in[0].record(s_in)
+    for i in range(steps):
+        b, nb = i % 2, (i + 1) % 2
+        if i + 1 < steps:
+            s_in.wait_event(ev_done[nb])
+            with torch.cuda.stream(s_in):
+                dA[nb].copy_(hA, non_blocking=True)
+                dB[nb].copy_(hB, non_blocking=True)
+                ev_in[nb].record(s_in)
+        comp.wait_event(ev_in[b])
+        comp.wait_event(ev_out[b])
+        api.gemm(dA[b], dB[b], "slice_bf16", out=dC[b], workspace=ws)
+        ev_done[b].record(comp)
+        s_out.wait_event(ev_done[b])
+        with torch.cuda.stream(s_out):
+            hC.copy_(dC[b], non_blocking=True)
+            ev_out[b].record(s_out)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    del dA, dB, dC, ws
+    torch.cuda.empty_cache()
+    return dt
 
 
 def bench_batched(api, inputs, stream):
@@ -336,27 +382,33 @@ def main():
     del pa_p, pb_p
     torch.cuda.empty_cache()
 
-    # ---- e2e through the C ABI with pinned host buffers
+    # ---- e2e through the C ABI's host-buffer call, pinned host buffers:
+    # every step copies A and B in, computes and copies C out
     hA = torch.from_numpy(A).pin_memory()
     hB = torch.from_numpy(B).pin_memory()
     hC = torch.empty((m, n, P), dtype=torch.float64).pin_memory()
+    del ws
+    torch.cuda.empty_cache()
 
     def e2e_step():
-        dA.copy_(hA, non_blocking=True)
-        dB.copy_(hB, non_blocking=True)
-        api.gemm(dA, dB, "slice_bf16", out=dC, workspace=ws)
-        hC.copy_(dC, non_blocking=True)
+        _lib.check(L.mdg_gemm_host(2, P, m, n, k, ctypes.c_void_p(hA.data_ptr()),
+                                   ctypes.c_void_p(hB.data_ptr()), ctypes.c_void_p(hC.data_ptr()),
+                                   None), "mdg_gemm_host")
 
     e2e_step()
-    torch.cuda.synchronize()
     e2e_steps = max(1, min(args.steps, 3))
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_step()
-    torch.cuda.synchronize()
     t_e2e = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world)
     assert np.array_equal(hC.numpy(), dC.cpu().numpy())
+    L.mdg_release_cache()
+
+    # ---- host link bandwidth and a pipelined host-to-host loop (copies of
+    # step i+1 and of the result of step i overlap the GEMM of step i)
+    t_h2d = event_time(lambda: dA.copy_(hA, non_blocking=True), stream, iters=2)
+    pipe = pipelined_e2e(api, hA, hB, hC, P, m, n, k, need, steps=max(2, min(args.steps, 3)))
 
     # ---- error bits on a sampled block against the exact product
     import oracle.exact as ex
@@ -406,7 +458,11 @@ def main():
                        "l2": "inputs (2 x 2 GiB) larger than L2, no flush"},
             "e2e": {"value": flops * world / t_e2e / 1e9, "unit": UNIT,
                     "h2d_bytes_per_step": A.nbytes + B.nbytes,
-                    "d2h_bytes_per_step": m * n * P * 8},
+                    "d2h_bytes_per_step": m * n * P * 8,
+                    "call": "mdg_gemm_host (pinned host buffers)",
+                    "h2d_gbs": A.nbytes / t_h2d / 1e9,
+                    "pipelined_value": flops * world / pipe / 1e9,
+                    "pipelined": "mdg_gemm on two device buffer sets; H2D of step i+1 and D2H of step i on copy streams overlap the GEMM of step i"},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_sust,
                          "unit": "TFLOP/s", "frac": achieved / bf16_sust, "traffic": None,
                          "kernel": "diag_gemm", "kernel_ms": t_diag * 1e3,

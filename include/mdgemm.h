@@ -63,7 +63,10 @@ typedef struct {
   int diagonals;    /* BF16 form: diagonals kept, 1..2*slices-1 (0: = slices) */
   int split_kind;   /* FP64 form: 0 split4 (pp=4P), 1 split8 (pp=8P), 2 mixed dd (pp=12) */
   int split_exact;  /* FP64 form: 0 or 1 = exact slices (default), 2 = reference-compatible */
-  int reserved[4];
+  int engine;       /* BF16 form: 0 auto, 1 tcgen05 128x256 tiles, 2 tcgen05 CTA pairs
+                       256x256, 3 mma.sync (legacy tensor path) */
+  int parts;        /* BF16 form, CTA pairs: diagonal ranges per tile (0: auto, 1..8) */
+  int reserved[2];
 } mdg_options;
 
 /* One problem of a batched call. */

@@ -16,7 +16,8 @@ c_int, c_ll, c_size, c_vp, c_char_p = (ctypes.c_int, ctypes.c_longlong, ctypes.c
 
 class Options(ctypes.Structure):
     _fields_ = [("slices", c_int), ("diagonals", c_int), ("split_kind", c_int),
-                ("split_exact", c_int), ("reserved", c_int * 4)]
+                ("split_exact", c_int), ("engine", c_int), ("parts", c_int),
+                ("reserved", c_int * 2)]
 
 
 class Problem(ctypes.Structure):

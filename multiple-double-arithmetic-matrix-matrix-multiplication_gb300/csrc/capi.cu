@@ -25,6 +25,21 @@ int default_engine() {
   return 1;
 }
 
+// Option value -> engine code of run_slice_gemm: 0 mma.sync, 1 tcgen05
+// (auto tile shape), 2 tcgen05 single CTA, 3 tcgen05 CTA pairs.  The
+// MDG_SLICE_ENGINE / MDG_TC_PAIR environment variables override "auto".
+int engine_choice(int opt) {
+  switch (opt) {
+    case 1: return 2;
+    case 2: return 3;
+    case 3: return 0;
+  }
+  if (default_engine() == 0) return 0;
+  const char *pv = std::getenv("MDG_TC_PAIR");
+  if (pv && *pv == '0') return 2;
+  return 1;
+}
+
 // ------------------------------------------------------------------ cache --
 // Grow-only device buffers owned by the library, for calls that take no
 // workspace argument (mdg_gemm_host, mdg_scale_exponents).  One per slot.
@@ -73,7 +88,7 @@ static int check_gemm_args(int form, int p, int m, int n, int k, const void *A, 
 }
 
 struct Opts {
-  int slices, diagonals, split_kind, split_exact;
+  int slices, diagonals, split_kind, split_exact, engine, parts;
 };
 
 static int resolve_opts(int p, const mdg_options *o, Opts *r) {
@@ -82,6 +97,9 @@ static int resolve_opts(int p, const mdg_options *o, Opts *r) {
   r->split_kind = o ? o->split_kind : 0;
   if (o && (o->split_exact < 0 || o->split_exact > 2)) return MDG_ERROR_INVALID_FORM;
   r->split_exact = (o && o->split_exact == 2) ? 0 : 1;
+  r->engine = o ? o->engine : 0;
+  r->parts = o ? o->parts : 0;
+  if (r->engine < 0 || r->engine > 3 || r->parts < 0 || r->parts > 8) return MDG_ERROR_INVALID_FORM;
   if (r->slices < 1 || r->slices > 128) return MDG_ERROR_INVALID_FORM;
   if (r->diagonals < 1 || r->diagonals > 2 * r->slices - 1) return MDG_ERROR_INVALID_FORM;
   if (r->split_kind < 0 || r->split_kind > 2) return MDG_ERROR_INVALID_FORM;
@@ -221,7 +239,8 @@ int mdg_gemm(int form, int p, int m, int n, int k, const double *A, int lda, con
     return run_split_gemm(p, o, m, n, k, A, lda, B, ldb, C, ldc, workspace, st);
   const SlicePlan pl = make_slice_plan(p, o.slices, o.diagonals, m, n, k);
   if (pl.Mp > 65535 || pl.Np > 65535) return MDG_ERROR_NOT_SUPPORTED;
-  return run_slice_gemm(pl, A, lda, B, ldb, C, ldc, workspace, default_engine(), st);
+  return run_slice_gemm(pl, A, lda, B, ldb, C, ldc, workspace, engine_choice(o.engine), o.parts,
+                        st);
 }
 
 int mdg_gemm_host(int form, int p, int m, int n, int k, const double *A, const double *B,
@@ -421,9 +440,10 @@ int mdg_slice_diagonals(int s, int D, int m, int n, int k, const void *dA, const
   if (m == 0 || n == 0 || k == 0) return MDG_SUCCESS;
   if (!dA || !dB || !chunks) return MDG_ERROR_NULL_POINTER;
   const long long plane_c = (long long)m * n;
-  if (default_engine() == 1 && ld == k)
+  const int eng = engine_choice(0);
+  if (eng != 0 && ld == k)
     return launch_diag_gemm_tc(s, D, m, n, k, dA, dB, ld, plane_a, plane_b, chunks, plane_c,
-                               as_stream(stream));
+                               eng == 2 ? 1 : 0, 0, as_stream(stream));
   return launch_diag_gemm_v0(s, D, m, n, k, dA, dB, ld, plane_a, plane_b, chunks, plane_c,
                              as_stream(stream));
 }

@@ -750,15 +750,13 @@ namespace mdgi {
 
 int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, const void *dB,
                         int ld, long long plane_a, long long plane_b, int *chunks,
-                        long long plane_c, cudaStream_t st) {
+                        long long plane_c, int single, int parts_opt, cudaStream_t st) {
   if (Mp % TM || Np % TN || Kp % TK || ld != Kp) return MDG_ERROR_INVALID_SIZE;
   if (plane_a != (long long)Mp * Kp || plane_b != (long long)Np * Kp) return MDG_ERROR_INVALID_SIZE;
   if ((reinterpret_cast<uintptr_t>(dA) | reinterpret_cast<uintptr_t>(dB)) & 15)
     return MDG_ERROR_INVALID_SIZE;
-  // the CTA-pair kernel needs 256-row tiles; MDG_TC_PAIR=0 selects the
-  // single-CTA kernel
-  const char *pv = std::getenv("MDG_TC_PAIR");
-  const bool pair = (Mp % 256 == 0) && !(pv && *pv == '0');
+  // the CTA-pair kernel needs 256-row tiles
+  const bool pair = (Mp % 256 == 0) && !single;
   CUtensorMap ma, mb;
   MDG_TRY(make_map(&ma, dA, Kp, (long long)s * Mp, TM));
   MDG_TRY(make_map(&mb, dB, Kp, (long long)s * Np, pair ? BH : TN));
@@ -791,8 +789,7 @@ int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, co
         parts = u;
       }
     }
-    const char *pe = std::getenv("MDG_TC_PARTS");
-    if (pe && *pe) parts = std::max(1, std::min(8, std::atoi(pe)));
+    if (parts_opt > 0) parts = std::min(8, parts_opt);
     const long long units = (long long)tiles * parts;
     const int clusters = units < ncl ? (int)units : ncl;
     diag_gemm_tc2_kernel<<<2 * clusters, THREADS, SMEM2_BYTES, st>>>(
