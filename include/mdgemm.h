@@ -66,7 +66,9 @@ typedef struct {
   int engine;       /* BF16 form: 0 auto, 1 tcgen05 128x256 tiles, 2 tcgen05 CTA pairs
                        256x256, 3 mma.sync (legacy tensor path) */
   int parts;        /* BF16 form, CTA pairs: diagonal ranges per tile (0: auto, 1..8) */
-  int reserved[2];
+  int raster;       /* BF16 form, CTA pairs: tile order runs across strips this many
+                       256-column blocks wide (0: auto) */
+  int reserved;
 } mdg_options;
 
 /* One problem of a batched call. */

@@ -21,11 +21,13 @@ SPLIT_KINDS = {"split4": 0, "split8": 1, "mix": 2}
 ENGINES = {"auto": 0, "tc": 1, "tc_pair": 2, "mma_sync": 3}
 
 
-def _opts(slices=0, diagonals=0, split_kind="split4", split_exact=True, engine="auto", parts=0):
+def _opts(slices=0, diagonals=0, split_kind="split4", split_exact=True, engine="auto", parts=0,
+          raster=0):
     o = Options()
     o.slices, o.diagonals = int(slices), int(diagonals)
     o.engine = ENGINES[engine] if isinstance(engine, str) else int(engine)
     o.parts = int(parts)
+    o.raster = int(raster)
     o.split_kind = SPLIT_KINDS[split_kind] if isinstance(split_kind, str) else int(split_kind)
     o.split_exact = 1 if split_exact else 2
     return o

@@ -88,7 +88,7 @@ static int check_gemm_args(int form, int p, int m, int n, int k, const void *A, 
 }
 
 struct Opts {
-  int slices, diagonals, split_kind, split_exact, engine, parts;
+  int slices, diagonals, split_kind, split_exact, engine, parts, raster;
 };
 
 static int resolve_opts(int p, const mdg_options *o, Opts *r) {
@@ -99,7 +99,9 @@ static int resolve_opts(int p, const mdg_options *o, Opts *r) {
   r->split_exact = (o && o->split_exact == 2) ? 0 : 1;
   r->engine = o ? o->engine : 0;
   r->parts = o ? o->parts : 0;
-  if (r->engine < 0 || r->engine > 3 || r->parts < 0 || r->parts > 8) return MDG_ERROR_INVALID_FORM;
+  r->raster = o ? o->raster : 0;
+  if (r->engine < 0 || r->engine > 3 || r->parts < 0 || r->parts > 8 || r->raster < 0)
+    return MDG_ERROR_INVALID_FORM;
   if (r->slices < 1 || r->slices > 128) return MDG_ERROR_INVALID_FORM;
   if (r->diagonals < 1 || r->diagonals > 2 * r->slices - 1) return MDG_ERROR_INVALID_FORM;
   if (r->split_kind < 0 || r->split_kind > 2) return MDG_ERROR_INVALID_FORM;
@@ -240,7 +242,7 @@ int mdg_gemm(int form, int p, int m, int n, int k, const double *A, int lda, con
   const SlicePlan pl = make_slice_plan(p, o.slices, o.diagonals, m, n, k);
   if (pl.Mp > 65535 || pl.Np > 65535) return MDG_ERROR_NOT_SUPPORTED;
   return run_slice_gemm(pl, A, lda, B, ldb, C, ldc, workspace, engine_choice(o.engine), o.parts,
-                        st);
+                        o.raster, st);
 }
 
 int mdg_gemm_host(int form, int p, int m, int n, int k, const double *A, const double *B,
@@ -443,7 +445,7 @@ int mdg_slice_diagonals(int s, int D, int m, int n, int k, const void *dA, const
   const int eng = engine_choice(0);
   if (eng != 0 && ld == k)
     return launch_diag_gemm_tc(s, D, m, n, k, dA, dB, ld, plane_a, plane_b, chunks, plane_c,
-                               eng == 2 ? 1 : 0, 0, as_stream(stream));
+                               eng == 2 ? 1 : 0, 0, 0, as_stream(stream));
   return launch_diag_gemm_v0(s, D, m, n, k, dA, dB, ld, plane_a, plane_b, chunks, plane_c,
                              as_stream(stream));
 }

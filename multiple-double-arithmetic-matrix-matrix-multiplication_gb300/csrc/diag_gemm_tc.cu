@@ -24,6 +24,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 
 #include "common.cuh"
@@ -270,9 +271,9 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
       // ------------------------------------------------------ producer --
       int st = 0;
       uint32_t ph = 0;
-      uint32_t last_par[STAGES];
-      bool issued[STAGES];
-      for (int i = 0; i < STAGES; ++i) issued[i] = false;
+      // per stage: a copy was issued (bit of `issued`), parity of its phase
+      // (bit of `last_par`); bit masks so that they stay in registers
+      uint32_t issued = 0, last_par = 0;
       for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const TileJob jb = jobs.job(tile);
         const int s = jb.s, KB = jb.KB;
@@ -286,8 +287,8 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
             const uint32_t a_dst = smem_base + st * STAGE_BYTES;
             tma_load_2d(a_dst, jb.tmA, kb * TK, i * jb.Mp + jb.row, full(st));
             tma_load_2d(a_dst + A_BYTES, jb.tmB, kb * TK, j * jb.Np + jb.col, full(st));
-            last_par[st] = ph;
-            issued[st] = true;
+            last_par = (last_par & ~(1u << st)) | (ph << st);
+            issued |= 1u << st;
             if (++st == STAGES) {
               st = 0;
               ph ^= 1;
@@ -298,7 +299,7 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
     producer_done:
       if (*abort_flag)
         for (int i = 0; i < STAGES; ++i)
-          if (issued[i]) mbar_drain(full(i), last_par[i]);
+          if ((issued >> i) & 1u) mbar_drain(full(i), (last_par >> i) & 1u);
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -504,17 +505,66 @@ __device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
                : "memory");
 }
 
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
+// Pacing across clusters.  Clusters that keep the same pace read the same
+// k-blocks of the same digit planes at about the same time, so each block
+// comes from DRAM once and from L2 for the others; left alone they drift
+// apart by more than L2 holds and most blocks come from DRAM again.  An
+// eleventh warp of the even CTA (the pacer) publishes its producer's
+// progress (k-steps issued, tagged with the launch's epoch) to a slot per
+// cluster and posts, in shared memory, how far the producer may go: the
+// slowest running cluster's progress plus `pace` k-steps.  The producer
+// holds before a k-step beyond that.  Only the timing depends on it: a hold
+// longer than PACE_WAIT_NS turns the pacing off for the rest of the launch
+// in that CTA, so a cluster that is not resident (or a concurrent launch
+// using the slots) costs at most that.
+constexpr int PACE_EVERY = 32, PACE_SLOTS = 128;
+constexpr int PACER_WARP = 2 + EPI_WARPS, THREADS2 = THREADS + 32;
+constexpr unsigned long long PACE_WAIT_NS = 50000, PACE_STALE_NS = 2000000000ull;
+constexpr uint32_t PACE_DONE = 0xFFFFFFFFu;
+// 64 and 128 k-steps ran equally well on quad-double 4096^3 and 8192^3
+// (8192^3: 289 ms per GEMM paced, 326 ms unpaced); 32 holds too often
+constexpr int kDefaultPace = 64;
+// one slot per 128-byte line, so that the clusters' stores and the pacers'
+// polling spread over L2 slices instead of contending for a few lines
+constexpr int PACE_STRIDE = 16;
+constexpr unsigned PACE_POLL_NS = 2000;
+__device__ unsigned long long g_pace[PACE_SLOTS * PACE_STRIDE];
+
+__device__ __forceinline__ void pace_publish(int slot, uint32_t epoch, uint32_t steps) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(g_pace + slot * PACE_STRIDE),
+               "l"(((unsigned long long)epoch << 32) | steps)
+               : "memory");
+}
+
+// Published progress of a cluster in this launch (0 before it publishes).
+__device__ __forceinline__ uint32_t pace_load(int slot, int ncl, uint32_t epoch) {
+  if (slot >= ncl) return PACE_DONE;
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];"
+               : "=l"(v)
+               : "l"(g_pace + slot * PACE_STRIDE)
+               : "memory");
+  return (uint32_t)(v >> 32) == epoch ? (uint32_t)v : 0u;
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
     diag_gemm_tc2_kernel(const __grid_constant__ CUtensorMap tmA,
                          const __grid_constant__ CUtensorMap tmB, int s, int D, int Mp, int Np,
-                         int KB, int *__restrict__ out, long long plane_c, int parts) {
+                         int KB, int *__restrict__ out, long long plane_c, int parts,
+                         int raster, int pace, uint32_t epoch) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES2 * STAGE2_BYTES);
-  // bars: [0,6) full, [6,12) empty, [12,14) accfull, [14,16) accempty, 16 drain
-  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bars + 20);
-  volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 21);
+  // bars: STAGES2 full, STAGES2 empty, 2 accfull, 2 accempty, 1 drain, then
+  // the TMEM address and the abort flag
+  static_assert(2 * STAGES2 + 9 <= 32, "barrier area holds 32 words of 8 bytes");
+  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bars + 2 * STAGES2 + 5);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 2 * STAGES2 + 6);
+  // pacing: k-steps issued by the producer (every PACE_EVERY), k-steps it
+  // may issue (posted by the pacer warp)
+  volatile uint32_t *pace_steps = reinterpret_cast<volatile uint32_t *>(bars + 2 * STAGES2 + 7);
+  volatile uint32_t *pace_allowed = reinterpret_cast<volatile uint32_t *>(bars + 2 * STAGES2 + 8);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t rank = cluster_rank();
@@ -537,6 +587,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
     }
     mbar_init(drain_bar, 1);
     *abort_flag = 0;
+    *pace_steps = 0;
+    *pace_allowed = PACE_DONE;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -555,6 +607,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
   const int tiles = MB * (Np / TN2);
   const int units = tiles * parts;
   const int cid = blockIdx.x >> 1, ncl = gridDim.x >> 1;
+  const bool pacer = leader && pace > 0 && ncl <= PACE_SLOTS;
   // a unit is one part of one tile: the diagonals [d0, d1) whose digit-pair
   // counts add up to about 1/parts of the tile's work
   auto unit_range = [&](int u, int &tile, int &d0, int &d1) {
@@ -576,44 +629,73 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
     }
     if (d0 > d1) d0 = d1;
   };
+  // tile -> (row block, column block).  Tiles run across a strip of
+  // `raster` column blocks, then down the rows, so that the clusters busy at
+  // the same time read few distinct A row blocks and B column blocks and
+  // share them in L2.  raster = 1 walks each column block top to bottom.
+  auto tile_rc = [&](int tile, int &rb, int &cb) {
+    const int NB = Np / TN2;
+    const int strip = tile / (MB * raster);
+    const int idx = tile - strip * MB * raster;
+    const int c0 = strip * raster;
+    const int g = NB - c0 < raster ? NB - c0 : raster;
+    rb = idx / g;
+    cb = c0 + idx - rb * g;
+  };
 
   if (warp == 0) {
     if (lane == 0) {
       // ------------------------------------------------------ producer --
       int st = 0;
       uint32_t ph = 0;
-      uint32_t last_par[STAGES2];
-      bool issued[STAGES2];
-      for (int i = 0; i < STAGES2; ++i) issued[i] = false;
+      // per stage: a copy was issued (bit of `issued`), parity of its phase
+      // (bit of `last_par`); bit masks so that they stay in registers
+      uint32_t issued = 0, last_par = 0;
+      bool pacing = pacer;
+      uint32_t steps = 0;  // k-steps issued by this cluster
       for (int u = cid; u < units; u += ncl) {
         int tile, d0, d1;
         unit_range(u, tile, d0, d1);
-        const int row = (tile % MB) * 256 + (int)rank * TM;
-        const int col = (tile / MB) * TN2 + (int)rank * BH;
+        int rb, cb;
+        tile_rc(tile, rb, cb);
+        const int row = rb * 256 + (int)rank * TM;
+        const int col = cb * TN2 + (int)rank * BH;
         for (int d = d0; d < d1; ++d) {
           const int ilo = d - (s - 1) > 0 ? d - (s - 1) : 0;
           const int S = mdgi::diag_pairs(d, s) * KB;
           for (int t = 0; t < S; ++t) {
             const int i = ilo + t / KB, kb = t - (t / KB) * KB, j = d - i;
+            if (pacing && steps > *pace_allowed) {
+              const unsigned long long t0 = now_ns();
+              while (steps > *pace_allowed) {
+                if (*abort_flag) break;
+                if (now_ns() - t0 > PACE_WAIT_NS) {
+                  pacing = false;
+                  break;
+                }
+              }
+            }
             if (!mbar_wait(empty(st), ph ^ 1, abort_flag)) goto producer_done;
             if (leader) mbar_expect_tx(full(st), 2 * STAGE2_BYTES);
             const uint32_t a_dst = smem_base + st * STAGE2_BYTES;
             const uint32_t bar0 = map_to_rank0(full(st));
             tma_load_2d_pair(a_dst, &tmA, kb * TK, i * Mp + row, bar0);
             tma_load_2d_pair(a_dst + A2_BYTES, &tmB, kb * TK, j * Np + col, bar0);
-            last_par[st] = ph;
-            issued[st] = true;
+            last_par = (last_par & ~(1u << st)) | (ph << st);
+            issued |= 1u << st;
             if (++st == STAGES2) {
               st = 0;
               ph ^= 1;
             }
+            if ((++steps & (PACE_EVERY - 1)) == 0) *pace_steps = steps;
           }
         }
       }
     producer_done:
+      *pace_steps = PACE_DONE;
       if (*abort_flag && leader)
         for (int i = 0; i < STAGES2; ++i)
-          if (issued[i]) mbar_drain(full(i), last_par[i]);
+          if ((issued >> i) & 1u) mbar_drain(full(i), (last_par >> i) & 1u);
     }
   } else if (warp == 1) {
     if (lane == 0 && leader) {
@@ -658,6 +740,39 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
         mbar_drain(drain_bar, 0);
       }
     }
+  } else if (warp == PACER_WARP) {
+    if (pacer) {
+      // --------------------------------------------------------- pacer --
+      // publishes the producer's progress and posts the number of k-steps
+      // it may issue (slowest running cluster + pace) until the producer
+      // is done; bounded by PACE_STALE_NS without news from the producer
+      uint32_t last = 0;
+      unsigned long long t_last = now_ns();
+      while (true) {
+        const uint32_t mine = __shfl_sync(0xffffffffu, *pace_steps, 0);
+        if (mine != last) {
+          last = mine;
+          t_last = now_ns();
+        }
+        if (lane == 0) pace_publish(cid, epoch, mine);
+        if (mine == PACE_DONE) break;
+        uint32_t m = PACE_DONE;
+#pragma unroll
+        for (int k = 0; k < PACE_SLOTS / 32; ++k) m = min(m, pace_load(lane + 32 * k, ncl, epoch));
+        m = __reduce_min_sync(0xffffffffu, m);
+        if (lane == 0)
+          *pace_allowed = m == PACE_DONE || m > PACE_DONE - (uint32_t)pace ? PACE_DONE
+                                                                           : m + (uint32_t)pace;
+        int stop = 0;
+        if (lane == 0) stop = (*abort_flag || now_ns() - t_last > PACE_STALE_NS) ? 1 : 0;
+        if (__shfl_sync(0xffffffffu, stop, 0)) break;
+        __nanosleep(PACE_POLL_NS);
+      }
+      if (lane == 0) {
+        *pace_allowed = PACE_DONE;
+        pace_publish(cid, epoch, PACE_DONE);
+      }
+    }
   } else {
     // -------------------------------------------------------- epilogue --
     const int q = warp & 3, h = (warp - 2) >> 2;
@@ -670,8 +785,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
     for (int u = cid; u < units; u += ncl) {
       int tile, d0, d1;
       unit_range(u, tile, d0, d1);
-      const int row = (tile % MB) * 256 + (int)rank * TM + 32 * q + lane;
-      const int col = (tile / MB) * TN2 + 128 * h;
+      int rb, cb;
+      tile_rc(tile, rb, cb);
+      const int row = rb * 256 + (int)rank * TM + 32 * q + lane;
+      const int col = cb * TN2 + 128 * h;
       int chunk = 0;
       for (int d = 0; d < d0; ++d) chunk += mdgi::diag_chunks(d, s, KB);
       for (int d = d0; d < d1; ++d) {
@@ -750,7 +867,8 @@ namespace mdgi {
 
 int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, const void *dB,
                         int ld, long long plane_a, long long plane_b, int *chunks,
-                        long long plane_c, int single, int parts_opt, cudaStream_t st) {
+                        long long plane_c, int single, int parts_opt, int raster_opt,
+                        cudaStream_t st) {
   if (Mp % TM || Np % TN || Kp % TK || ld != Kp) return MDG_ERROR_INVALID_SIZE;
   if (plane_a != (long long)Mp * Kp || plane_b != (long long)Np * Kp) return MDG_ERROR_INVALID_SIZE;
   if ((reinterpret_cast<uintptr_t>(dA) | reinterpret_cast<uintptr_t>(dB)) & 15)
@@ -776,24 +894,43 @@ int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, co
   if (pair) {
     const int tiles = (Mp / 256) * (Np / TN2);
     // split tiles into `parts` diagonal ranges when that shrinks the idle
-    // part of the last wave of clusters
+    // part of the last wave of clusters by more than it costs: each extra
+    // part makes the work about 4 % slower (fitted to quad-double 4096^3 and
+    // 8192^3: 1024 tiles on 76 clusters run best unsplit, 256 tiles best in
+    // two parts)
     const int ncl = sms / 2;
     int parts = 1;
-    double best = 2.0;
+    double best = 0.0;
     for (int u = 1; u <= 8 && u <= D; ++u) {
       const long long units = (long long)tiles * u;
       const long long waves = (units + ncl - 1) / ncl;
-      const double waste = (double)(waves * ncl - units) / (double)(waves * ncl);
-      if (waste < best - 0.01) {
-        best = waste;
+      const double cost = (double)waves / u * (1.0 + 0.04 * (u - 1));
+      if (u == 1 || cost < best) {
+        best = cost;
         parts = u;
       }
     }
     if (parts_opt > 0) parts = std::min(8, parts_opt);
+    // tile order: strips about sqrt(clusters) column blocks wide, so that
+    // the tiles in work at one time span few row and column blocks (the
+    // largest power of two not above sqrt(76) = 8.7 on 152 SMs)
+    const int NB = Np / TN2;
+    int raster = 1;
+    while ((raster * 2) * (raster * 2) <= ncl) raster *= 2;
+    if (raster_opt > 0) raster = raster_opt;
+    raster = std::min(NB, raster);
     const long long units = (long long)tiles * parts;
     const int clusters = units < ncl ? (int)units : ncl;
-    diag_gemm_tc2_kernel<<<2 * clusters, THREADS, SMEM2_BYTES, st>>>(
-        ma, mb, s, D, Mp, Np, Kp / TK, chunks, plane_c, parts);
+    // pacing window in k-steps, 0 = off (MDG_TC_PACE overrides); every
+    // launch gets its own epoch so that slots left by earlier launches read
+    // as "not started"
+    int pace = kDefaultPace;
+    if (const char *e = std::getenv("MDG_TC_PACE")) pace = std::max(0, std::atoi(e));
+    static std::atomic<uint32_t> epochs{0};
+    uint32_t epoch = ++epochs;
+    if (epoch == 0) epoch = ++epochs;
+    diag_gemm_tc2_kernel<<<2 * clusters, THREADS2, SMEM2_BYTES, st>>>(
+        ma, mb, s, D, Mp, Np, Kp / TK, chunks, plane_c, parts, raster, pace, epoch);
   } else {
     const int tiles = (Mp / TM) * (Np / TN);
     const int grid = tiles < sms ? tiles : sms;

@@ -75,7 +75,8 @@ int mdg_gemm_slice_static(int p, int m, int n, int k, const double *A, int lda, 
   }
   void *scratch = nullptr;
   MDG_TRY(scratch_address(&scratch));
-  return mdgi::run_slice_gemm(pl, A, lda, B, ldb, C, ldc, scratch, mdgi::engine_choice(0), 0, st);
+  return mdgi::run_slice_gemm(pl, A, lda, B, ldb, C, ldc, scratch, mdgi::engine_choice(0), 0, 0,
+                              st);
 }
 
 }  // extern "C"

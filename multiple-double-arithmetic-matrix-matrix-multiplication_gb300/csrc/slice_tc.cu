@@ -372,7 +372,8 @@ int launch_renorm(int p, int s, int D, int KB, int m, int n, const int *chunks,
 }
 
 int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *B, int ldb,
-                   double *C, int ldc, void *ws, int engine, int parts, cudaStream_t st) {
+                   double *C, int ldc, void *ws, int engine, int parts, int raster,
+                   cudaStream_t st) {
   char *base = reinterpret_cast<char *>(ws);
   auto *rowbits = reinterpret_cast<unsigned long long *>(base + pl.off_rowbits);
   auto *colbits = reinterpret_cast<unsigned long long *>(base + pl.off_colbits);
@@ -389,7 +390,7 @@ int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *
                         pl.Kp, st));
   if (engine != 0) {
     MDG_TRY(launch_diag_gemm_tc(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
-                                pl.plane_b, Cd, pl.plane_c, engine == 2 ? 1 : 0, parts, st));
+                                pl.plane_b, Cd, pl.plane_c, engine == 2 ? 1 : 0, parts, raster, st));
   } else {
     MDG_TRY(launch_diag_gemm_v0(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
                                 pl.plane_b, Cd, pl.plane_c, st));

@@ -55,10 +55,11 @@ int launch_diag_gemm_v0(int s, int D, int Mp, int Np, int Kp, const void *dA, co
                         long long plane_c, cudaStream_t st);
 // tcgen05 engine (Mp % 128, Np % 256, Kp % 64, ld == Kp).  single: 1 forces
 // 128 x 256 tiles on one CTA, 0 uses CTA pairs when Mp % 256 == 0.  parts:
-// diagonal ranges per pair tile, 0 = chosen to fill the last wave.
+// diagonal ranges per pair tile, 0 = chosen to fill the last wave.  raster:
+// pair tiles run across strips this many 256-column blocks wide (0 = auto).
 int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, const void *dB,
                         int ld, long long plane_a, long long plane_b, int *chunks,
-                        long long plane_c, int single, int parts, cudaStream_t st);
+                        long long plane_c, int single, int parts, int raster, cudaStream_t st);
 int launch_renorm(int p, int s, int D, int KB, int m, int n, const int *chunks,
                   long long plane_c, int ldcd, const int *E, const int *F, double *C, int ldc,
                   cudaStream_t st);
@@ -83,7 +84,8 @@ int tc_device_status();
 // engine: 0 = mma.sync, 1 = tcgen05 auto tiles, 2 = tcgen05 single CTA,
 // 3 = tcgen05 CTA pairs
 int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *B, int ldb,
-                   double *C, int ldc, void *ws, int engine, int parts, cudaStream_t st);
+                   double *C, int ldc, void *ws, int engine, int parts, int raster,
+                   cudaStream_t st);
 
 // Which engine mdg_gemm uses for the BF16 form (MDG_SLICE_ENGINE=0/1 overrides).
 int default_engine();

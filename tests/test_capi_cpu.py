@@ -75,3 +75,25 @@ def test_workspace_sizes(L):
     # digits of A and B (28 planes of 128 x 64 BF16) + 28 diagonal planes
     assert ws_tc >= 2 * 28 * 128 * 64 * 2 + 28 * 128 * 128 * 8
     assert api.workspace_size("slice_bf16", 4, 64, 64, 64, slices=200) == 0
+
+
+@pytest.mark.parametrize("field,value", [("engine", 4), ("engine", -1), ("parts", 9), ("parts", -1),
+                                         ("raster", -1), ("split_exact", 3)])
+def test_bad_options_rejected(L, field, value):
+    """Out-of-range mdg_options fields: no workspace size, and mdg_gemm
+    returns MDG_ERROR_INVALID_FORM before touching the device."""
+    api = pkg("api")
+    o = api._opts()
+    setattr(o, field, value)
+    assert L.mdg_gemm_workspace_size(2, 4, 64, 64, 64, ctypes.byref(o)) == 0
+    one = ctypes.c_void_p(1)
+    assert L.mdg_gemm(2, 4, 4, 4, 4, one, 4, one, 4, one, 4, ctypes.byref(o), None, 0, None) == 4
+
+
+def test_schedule_options_accepted(L):
+    """parts, raster and engine choices inside their ranges resolve."""
+    api = pkg("api")
+    base = api.workspace_size("slice_bf16", 4, 512, 512, 512)
+    for kw in ({"engine": "tc_pair", "parts": 8, "raster": 1000}, {"engine": "mma_sync"},
+               {"engine": "tc", "parts": 1, "raster": 1}):
+        assert api.workspace_size("slice_bf16", 4, 512, 512, 512, **kw) == base

@@ -248,6 +248,25 @@ def test_slice_gemm_bit_exact_against_oracle(api, orc, inputs, engine, P, shape,
     assert np.array_equal(got, orc.gemm_slices(P, s, s, A, B, m, n, k))
 
 
+def test_slice_gemm_schedules_bit_identical(api, inputs, monkeypatch):
+    """Tile order (raster), diagonal ranges per tile (parts) and the pacing
+    of the CTA-pair kernel only reorder exact integer work: every schedule,
+    and the mma.sync engine, must return the same bits.  36 pair tiles with
+    2560-deep k (diagonals span two int32 chunks); pace 1 makes the
+    producers hold at almost every check."""
+    P, m, n, k = 4, 1536, 1536, 2560
+    rng = np.random.default_rng(1536)
+    A = dev(inputs.normal_pd(rng, (m, k), P))
+    B = dev(inputs.normal_pd(rng, (k, n), P))
+    ref = host(api.gemm(A, B, "slice_bf16", engine="mma_sync"))
+    for pace in ("0", "1", "64"):
+        monkeypatch.setenv("MDG_TC_PACE", pace)
+        for parts, raster in ((0, 0), (1, 1), (3, 2), (2, 5), (8, 100)):
+            got = host(api.gemm(A, B, "slice_bf16", engine="tc_pair", parts=parts, raster=raster))
+            assert np.array_equal(got, ref), (pace, parts, raster)
+    assert api.device_status() == 0
+
+
 def test_slice_gemm_hexa_double_bit_exact(api, orc, inputs):
     """P = 16 through the BF16 form (108 digits, 5886 digit pairs)."""
     rng = np.random.default_rng(16)
