@@ -157,12 +157,20 @@ int mdg_gemm_slice_static(int p, int m, int n, int k, const double *A, int lda,
 /* ------------------------------------------------- FP64 split stages -- */
 
 /* Slices of `count` P-doubles: kind 0 split4pd (floatybits.cu:196),
- * 1 split8pd (:303), 2 mixsplit2 (:327, P must be 2).  exact = 0 gives the
- * reference's slices bit for bit, quirks included (a negative limb gives
- * zero slices, the 53rd significand bit is dropped); exact = 1 keeps sign
- * and all bits.  out: count x pp doubles (pp = 4P, 8P or 12). */
+ * 1 split8pd (:303), 2 mixsplit2 (:327, P must be 2), 3 the unbalanced
+ * split4pd of the CPU convolution driver (TCcudant.cpp:163).  exact = 0
+ * gives the reference's slices bit for bit, quirks included (a negative
+ * limb gives zero slices, the 53rd significand bit is dropped); exact = 1
+ * keeps sign and all bits.  out: count x pp doubles (pp = 4P, 8P, 12, 4P). */
 int mdg_split(int kind, int exact, int p, long long count, const double *x,
               double *out, void *stream);
+
+/* The same slices as pp planes: slice j of entry e at planes[j * plane_stride
+ * + e], plane_stride >= count.  With kind 3 this is splitp(split4pd(x), 4P)
+ * of TCcudant.cpp:163-183 (without splitp's read one element past the end,
+ * which shifts every plane after the first by one entry there). */
+int mdg_split_planes(int kind, int exact, int p, long long count, const double *x,
+                     double *planes, long long plane_stride, void *stream);
 
 /* y_i = sum_j x[i*pp + j] through the P-double inc_d, j in order; y is
  * count x P.  Replaces pllsqueeze_old (TCcuda.cu:908) and its kernels
@@ -178,6 +186,15 @@ size_t mdg_slice_conv_workspace_size(int pp, int m, int n, int k);
 int mdg_slice_conv(int pp, int m, int n, int k, const double *Aq,
                    const double *Bq, double *Cq, void *workspace,
                    size_t workspace_bytes, void *stream);
+
+/* The same convolution on slice planes, the layout of the CPU convolution
+ * driver: A is pp planes of m x k, B pp planes of k x n, C pp planes of
+ * m x n (all row-major, planes contiguous); C_i = sum_{j<=i} A_j B_{i-j}.
+ * Replaces manualconvmult (convmult2 + convadd2, TCcudant.cpp:216-250) and
+ * directdotconv (TCcudant.cpp:252-276), which compute it in FP64 on one
+ * core. */
+int mdg_plane_conv(int pp, int m, int n, int k, const double *A,
+                   const double *B, double *C, void *stream);
 
 /* ----------------------------------------------- BF16 slice stages -- */
 
@@ -219,6 +236,33 @@ int mdg_renorm_diagonals(int p, int s, int D, int k, int m, int n,
                          const int *chunks, long long plane_c, int ldcd,
                          const int *E, const int *F, double *C, int ldc,
                          void *stream);
+
+/* ---------------------------------------------------- input generator -- */
+
+/* Distributions of mdg_generate (low two bits of dist), and scale flags
+ * that may be OR'ed onto MDG_GEN_UNIFORM or MDG_GEN_NORMAL. */
+enum {
+  MDG_GEN_UNIFORM = 0,     /* hi limb U[-1, 1); limb i+1 = U[-1, 1) * ulp(limb i) / 2;
+                              then a bottom-up and a top-down quick-two-sum sweep */
+  MDG_GEN_NORMAL = 1,      /* as UNIFORM with a hi limb of mean 0 and variance 1: the
+                              Irwin-Hall sum of 12 uniforms minus 6, rounded once */
+  MDG_GEN_REFERENCE = 2,   /* the reference's random_pd family (floatybits.cu:107-120):
+                              limb i = f_i 2^(e - 52 i), f_i in [0.5, 1) with 52 fraction
+                              bits, the first set; e = e0 + U{0 .. e1 - e0 - 1} (e0 when
+                              e1 == e0); e0 >= -1021 + 52 (P - 1), e <= 1023 */
+  MDG_GEN_SCALE_ROWS = 4,  /* then multiply row r by 2^U{e0 .. e1}, -64 <= e0 <= e1 <= 64 */
+  MDG_GEN_SCALE_COLS = 8   /* then multiply column c by 2^U{e0 .. e1} (both flags: both) */
+};
+
+/* Fills the rows x cols P-double matrix X (device, leading dimension ldx
+ * in entries) from `seed` with a counter-based generator (splitmix64 of
+ * the seed, the entry index r * cols + c and the draw number): every entry
+ * depends only on those, so any device, any launch shape and the CPU give
+ * the same bits.  Builds inputs on the GPU instead of the host loops of
+ * random_pd / mat (floatybits.cu:107-120, TCcuda.cu:14-21), for callers
+ * that do not need the rand() sequence (the drop-in mat keeps it). */
+int mdg_generate(int dist, int p, int rows, int cols, unsigned long long seed,
+                 int e0, int e1, double *X, int ldx, void *stream);
 
 /* Waits for the device and reports MDG_ERROR_TIMEOUT when a bounded wait
  * inside a tensor-core kernel gave up since the previous call (the record

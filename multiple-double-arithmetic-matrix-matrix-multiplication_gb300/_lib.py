@@ -42,6 +42,8 @@ SIGNATURES = {
     "mdg_gemm_batched": (c_int, [c_int, _P_PROB, c_int, _P_OPT, c_vp, c_size, c_vp]),
     "mdg_release_cache": (None, []),
     "mdg_split": (c_int, [c_int, c_int, c_int, c_ll, c_vp, c_vp, c_vp]),
+    "mdg_split_planes": (c_int, [c_int, c_int, c_int, c_ll, c_vp, c_vp, c_ll, c_vp]),
+    "mdg_plane_conv": (c_int, [c_int] * 4 + [c_vp, c_vp, c_vp, c_vp]),
     "mdg_squeeze": (c_int, [c_int, c_int, c_ll, c_vp, c_vp, c_vp]),
     "mdg_slice_conv_workspace_size": (c_size, [c_int] * 4),
     "mdg_slice_conv": (c_int, [c_int] * 4 + [c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
@@ -52,6 +54,7 @@ SIGNATURES = {
     "mdg_renorm_diagonals": (c_int, [c_int] * 6 + [c_vp, c_ll, c_int, c_vp, c_vp, c_vp, c_int,
                                                    c_vp]),
     "mdg_device_status": (c_int, []),
+    "mdg_generate": (c_int, [c_int] * 4 + [ctypes.c_ulonglong, c_int, c_int, c_vp, c_int, c_vp]),
     "mdg_static_scratch_bytes": (c_size, []),
     "mdg_batch_workspace_size": (c_size, [_P_PROB, c_int]),
     "mdg_batch_create": (c_int, [_P_PROB, c_int, c_vp, c_size, c_vp, ctypes.POINTER(c_vp)]),

@@ -164,7 +164,7 @@ def matmulTCnt(A, B, n, nfrag, p, loop_ct=1):
 def _split(kind, x, p, exact=False):
     x = _dev(np.asarray(x, dtype=np.float64).reshape(-1, p)) if not isinstance(x, torch.Tensor) else x.contiguous()
     count = x.numel() // p
-    pp = {0: 4 * p, 1: 8 * p, 2: 12}[kind]
+    pp = {0: 4 * p, 1: 8 * p, 2: 12, 3: 4 * p}[kind]
     out = torch.empty((count, pp), dtype=torch.float64, device=x.device)
     check(lib().mdg_split(kind, int(exact), p, count, _ptr(x), _ptr(out), _stream(None)),
           "mdg_split")
@@ -183,6 +183,37 @@ def split8pd(x, p, exact=False):
 
 def mixsplit2(x, exact=False):
     return _split(2, x, 2, exact)
+
+
+def split4pd_unbalanced(x, p, exact=False):
+    """split4pd of the CPU convolution driver (TCcudant.cpp:163): the
+    split4 slices without balance4."""
+    return _split(3, x, p, exact)
+
+
+def split_planes(kind, x, p, exact=False):
+    """Slices as planes: (pp, count) with plane j holding slice j of every
+    entry; kind as in mdg_split (3 = splitp(split4pd(x), 4p) of
+    TCcudant.cpp:163-183)."""
+    x = _dev(np.asarray(x, dtype=np.float64).reshape(-1, p)) if not isinstance(x, torch.Tensor) else x.contiguous()
+    count = x.numel() // p
+    pp = {0: 4 * p, 1: 8 * p, 2: 12, 3: 4 * p}[kind]
+    out = torch.empty((pp, count), dtype=torch.float64, device=x.device)
+    check(lib().mdg_split_planes(kind, int(exact), p, count, _ptr(x), _ptr(out), count,
+                                 _stream(None)), "mdg_split_planes")
+    return out
+
+
+def plane_conv(A, B):
+    """C_i = sum_{j<=i} A_j B_{i-j} on slice planes (FP64 tensor cores); A
+    (pp, m, k), B (pp, k, n) device tensors -> C (pp, m, n): manualconvmult /
+    directdotconv of TCcudant.cpp:216-276."""
+    pp, m, k = A.shape
+    n = B.shape[2]
+    C = torch.empty((pp, m, n), dtype=torch.float64, device=A.device)
+    check(lib().mdg_plane_conv(pp, m, n, k, _ptr(A.contiguous()), _ptr(B.contiguous()), _ptr(C),
+                               _stream(None)), "mdg_plane_conv")
+    return C
 
 
 def pllsqueeze_old(x, p, pp):
@@ -268,3 +299,23 @@ def renorm_diagonals(Cd, E, F, p, s, D, k):
 
 def device_status():
     return lib().mdg_device_status()
+
+
+GEN_DISTS = {"uniform": 0, "normal": 1, "reference": 2}
+GEN_SCALE_ROWS, GEN_SCALE_COLS = 4, 8
+
+
+def generate(dist, p, rows, cols, seed, e0=0, e1=0, scale_rows=False, scale_cols=False,
+             out=None, stream=None):
+    """rows x cols P-double matrix (cuda tensor rows x cols x P) from the
+    counter-based generator mdg_generate: dist "uniform" / "normal" (hi limb
+    U[-1, 1) / mean 0, variance 1, tail limbs below the ulp, renormalised) or
+    "reference" (random_pd's family, exponents e0 .. e1 - 1); scale_rows /
+    scale_cols multiply rows / columns by 2^U{e0..e1}."""
+    d = GEN_DISTS[dist] | (GEN_SCALE_ROWS if scale_rows else 0) | (GEN_SCALE_COLS if scale_cols else 0)
+    if out is None:
+        out = torch.empty((rows, cols, p), dtype=torch.float64, device="cuda")
+    ld = out.stride(0) // p if out.dim() == 3 and rows > 1 else max(cols, 1)
+    check(lib().mdg_generate(d, p, rows, cols, int(seed) & (2 ** 64 - 1), e0, e1, _ptr(out), ld,
+                             _stream(stream)), "mdg_generate")
+    return out

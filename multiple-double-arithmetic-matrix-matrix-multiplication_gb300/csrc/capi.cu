@@ -161,7 +161,7 @@ static int run_split_gemm(int p, const Opts &o, int m, int n, int k, const doubl
   double *Cq = reinterpret_cast<double *>(base + sp.off_Cq);
   MDG_TRY(launch_split(o.split_kind, o.split_exact, p, (long long)m * k, Ac, Aq, 0, 0, st));
   MDG_TRY(launch_split(o.split_kind, o.split_exact, p, (long long)k * n, Bc, Bq, 0, 0, st));
-  MDG_TRY(launch_slice_conv(sp.pp, m, n, k, Aq, Bq, Cq, st));
+  MDG_TRY(launch_slice_conv(sp.pp, m, n, k, Aq, Bq, Cq, 0, st));
   double *Cout = (ldc == n) ? C : reinterpret_cast<double *>(base + sp.off_Cp);
   MDG_TRY(launch_squeeze(p, sp.pp, (long long)m * n, Cq, sp.pp, 1, Cout, st));
   if (ldc != n && m > 0 && n > 0) {
@@ -372,11 +372,21 @@ int mdg_gemm_batched(int form, const mdg_problem *problems, int count, const mdg
 int mdg_split(int kind, int exact, int p, long long count, const double *x, double *out,
               void *stream) {
   if (!valid_p(p)) return MDG_ERROR_INVALID_LIMBS;
-  if (kind < 0 || kind > 2 || (exact != 0 && exact != 1)) return MDG_ERROR_INVALID_FORM;
+  if (kind < 0 || kind > 3 || (exact != 0 && exact != 1)) return MDG_ERROR_INVALID_FORM;
   if (kind == 2 && p != 2) return MDG_ERROR_INVALID_LIMBS;
   if (count < 0) return MDG_ERROR_INVALID_SIZE;
   if (count > 0 && (!x || !out)) return MDG_ERROR_NULL_POINTER;
   return launch_split(kind, exact, p, count, x, out, 0, 0, as_stream(stream));
+}
+
+int mdg_split_planes(int kind, int exact, int p, long long count, const double *x,
+                     double *planes, long long plane_stride, void *stream) {
+  if (!valid_p(p)) return MDG_ERROR_INVALID_LIMBS;
+  if (kind < 0 || kind > 3 || (exact != 0 && exact != 1)) return MDG_ERROR_INVALID_FORM;
+  if (kind == 2 && p != 2) return MDG_ERROR_INVALID_LIMBS;
+  if (count < 0 || plane_stride < count) return MDG_ERROR_INVALID_SIZE;
+  if (count > 0 && (!x || !planes)) return MDG_ERROR_NULL_POINTER;
+  return launch_split(kind, exact, p, count, x, planes, 1, plane_stride, as_stream(stream));
 }
 
 int mdg_squeeze(int p, int pp, long long count, const double *x, double *y, void *stream) {
@@ -396,9 +406,17 @@ int mdg_slice_conv(int pp, int m, int n, int k, const double *Aq, const double *
   (void)workspace;
   (void)workspace_bytes_;
   if (pp < 1 || m < 0 || n < 0 || k < 0) return MDG_ERROR_INVALID_SIZE;
-  if ((m > 0 && n > 0 && !Cq) || (m > 0 && k > 0 && !Aq) || (k > 0 && n > 0 && !Bq))
-    return MDG_ERROR_NULL_POINTER;
-  return launch_slice_conv(pp, m, n, k, Aq, Bq, Cq, as_stream(stream));
+  if (m == 0 || n == 0) return MDG_SUCCESS;  // nothing is read or written
+  if (!Cq || (k > 0 && (!Aq || !Bq))) return MDG_ERROR_NULL_POINTER;
+  return launch_slice_conv(pp, m, n, k, Aq, Bq, Cq, 0, as_stream(stream));
+}
+
+int mdg_plane_conv(int pp, int m, int n, int k, const double *A, const double *B, double *C,
+                   void *stream) {
+  if (pp < 1 || m < 0 || n < 0 || k < 0) return MDG_ERROR_INVALID_SIZE;
+  if (m == 0 || n == 0) return MDG_SUCCESS;  // nothing is read or written
+  if (!C || (k > 0 && (!A || !B))) return MDG_ERROR_NULL_POINTER;
+  return launch_slice_conv(pp, m, n, k, A, B, C, 1, as_stream(stream));
 }
 
 int mdg_scale_exponents(int p, int m, int n, int k, const double *A, int lda, const double *B,

@@ -49,6 +49,7 @@ int launch_split(int kind, int exact, int p, long long count, const double *x, d
                  int soa, long long plane_stride, cudaStream_t st);
 int launch_squeeze(int p, int pp, long long count, const double *x, long long x_stride,
                    long long x_plane, double *y, cudaStream_t st);
+// planes = 0: AoS (m x k x pp, ...); 1: pp slice planes of m x k, k x n, m x n
 int launch_slice_conv(int pp, int m, int n, int k, const double *Aq, const double *Bq,
-                      double *Cq, cudaStream_t st);
+                      double *Cq, int planes, cudaStream_t st);
 }  // namespace mdgi

@@ -1,4 +1,5 @@
-// Drop-in C++ surface of the reference (TCcuda.h:23-103, floatybits.h:17-97)
+// Drop-in C++ surface of the reference (TCcuda.h:23-103, floatybits.h:17-97,
+// and the functions of the CPU convolution driver TCcudant.cpp:163-276)
 // over the C ABI.  std::vector in, std::vector out, like the reference; the
 // GPU work goes through mdg_* entry points.
 //
@@ -14,6 +15,7 @@
 #include <cstring>
 
 #include "TCcuda.h"
+#include "TCcudant.h"
 #include "common.cuh"
 
 namespace {
@@ -446,3 +448,88 @@ __global__ void pllsqueeze_2_pp_old(double *x, double *y, int pp) { squeeze_entr
 __global__ void pllsqueeze_4_pp_old(double *x, double *y, int pp) { squeeze_entry<4>(x, y, pp); }
 __global__ void pllsqueeze_8_pp_old(double *x, double *y, int pp) { squeeze_entry<8>(x, y, pp); }
 __global__ void pllsqueeze_16_pp_old(double *x, double *y, int pp) { squeeze_entry<16>(x, y, pp); }
+
+// ------------------------------------------------------------------------
+// The CPU convolution driver's functions (include/TCcudant.h,
+// TCcudant.cpp:163-276): slicing and FP64 plane products on the GPU.
+
+namespace {
+
+// C (pp planes of m x n) = the truncated convolution of A (pp planes of
+// m x k) and B (pp planes of k x n) through mdg_plane_conv; zeros if the
+// device cannot be used.
+vector<double> gpu_plane_conv(const vector<double> &A, const vector<double> &B, int pp, int m,
+                              int n, int k) {
+  vector<double> C((size_t)pp * m * n, 0.0);
+  if (pp <= 0 || m <= 0 || n <= 0) return C;
+  DevBuf dA(A.size()), dB(B.size()), dC(C.size());
+  if ((A.size() && !dA.p) || (B.size() && !dB.p) || !dC.p) return C;
+  cudaMemcpy(dA.p, A.data(), A.size() * sizeof(double), cudaMemcpyHostToDevice);
+  cudaMemcpy(dB.p, B.data(), B.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (mdg_plane_conv(pp, m, n, k, dA.p, dB.p, dC.p, nullptr) == MDG_SUCCESS)
+    cudaMemcpy(C.data(), dC.p, C.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  return C;
+}
+
+}  // namespace
+
+vector<double> zeros(int n, int p) { return vector<double>((size_t)n * n * p, 0.0); }
+
+vector<double> split4pd(vector<double> x) {
+  const long long count = (long long)x.size();
+  vector<double> out((size_t)count * 4, 0.0);
+  if (!count) return out;
+  DevBuf dx(x.size()), dout(out.size());
+  if (!dx.p || !dout.p) return out;
+  cudaMemcpy(dx.p, x.data(), x.size() * sizeof(double), cudaMemcpyHostToDevice);
+  // one double per entry (P = 1): the slices of each double on its own
+  if (mdgi::launch_split(3, 0, 1, count, dx.p, dout.p, 0, 0, nullptr) == MDG_SUCCESS)
+    cudaMemcpy(out.data(), dout.p, out.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  return out;
+}
+
+vector<double> splitp(vector<double> A, int p) {
+  if (p <= 0) return vector<double>();
+  const size_t cnt = A.size() / (size_t)p;
+  vector<double> out(cnt * (size_t)p);
+  for (int i = 0; i < p; ++i)
+    for (size_t e = 0; e < cnt; ++e) out[(size_t)i * cnt + e] = A[e * (size_t)p + i];
+  return out;
+}
+
+void matmul2(vector<double> A, vector<double> B, vector<double> &C, int n) {
+  const vector<double> P = gpu_plane_conv(A, B, 1, n, n, n);
+  for (size_t i = 0; i < P.size() && i < C.size(); ++i) C[i] += P[i];
+}
+
+void convmult2(vector<double> A, vector<double> B, vector<double> &C_aux, int n, int p) {
+  const size_t nn = (size_t)n * n;
+  for (int i = 0; i < p; ++i)
+    for (int j = 0; j < p; ++j) {
+      const vector<double> Ai(A.begin() + i * nn, A.begin() + (i + 1) * nn);
+      const vector<double> Bj(B.begin() + j * nn, B.begin() + (j + 1) * nn);
+      const vector<double> P = gpu_plane_conv(Ai, Bj, 1, n, n, n);
+      double *dst = C_aux.data() + ((size_t)i * p + j) * nn;
+      for (size_t e = 0; e < nn; ++e) dst[e] += P[e];
+    }
+}
+
+void convadd2(vector<double> &C, vector<double> &C_aux, int n, int p) {
+  const size_t nn = (size_t)n * n;
+  for (int i = 0; i < p; ++i)
+    for (size_t e = 0; e < nn; ++e)
+      for (int j = 0; j <= i; ++j) C[i * nn + e] += C_aux[((size_t)j * p + (i - j)) * nn + e];
+}
+
+vector<double> manualconvmult(vector<double> A, vector<double> B, int n, int p) {
+  return gpu_plane_conv(A, B, p, n, n, n);
+}
+
+void dotconvbutbetter(vector<double> A, vector<double> B, vector<double> &C, int n, int p) {
+  const vector<double> P = gpu_plane_conv(A, B, p, n, n, n);
+  for (size_t i = 0; i < P.size() && i < C.size(); ++i) C[i] += P[i];
+}
+
+vector<double> directdotconv(vector<double> A, vector<double> B, int n, int p) {
+  return gpu_plane_conv(A, B, p, n, n, n);
+}

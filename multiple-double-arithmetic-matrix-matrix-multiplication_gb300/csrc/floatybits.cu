@@ -4,7 +4,8 @@
 // ranges of its significand bits, then adjacent slices of one P-double are
 // "balanced" so that their exponents differ by at most 13 (or 7/6) bits.
 // Reference: split4 / split4pd / balance4 (floatybits.cu:134-206), split8 /
-// split8pd / balance8 (:208-313), mixsplit2 / mixbalance (:315-342).  The
+// split8pd / balance8 (:208-313), mixsplit2 / mixbalance (:315-342), and
+// the unbalanced split4pd of the CPU convolution driver (TCcudant.cpp:163).  The
 // reference goes through vector<int> bit arrays and pow() loops on the host;
 // here one thread per P-double reads the IEEE fields with frexp/ldexp.
 //
@@ -80,7 +81,7 @@ __global__ void split_kernel(int kind, int exact, int P, long long count,
                              long long plane_stride) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
-  const int pp = kind == 0 ? 4 * P : kind == 1 ? 8 * P : 12;
+  const int pp = (kind == 0 || kind == 3) ? 4 * P : kind == 1 ? 8 * P : 12;
   double w[128];
   int pos = 0;
   for (int l = 0; l < P; ++l) {
@@ -109,7 +110,8 @@ __global__ void split_kernel(int kind, int exact, int P, long long count,
     }
     pos += use8 ? 8 : 4;
   }
-  for (int j = 0; j + 1 < pp; ++j) {
+  // kind 3 (split4pd of TCcudant.cpp:163) keeps the slices unbalanced
+  for (int j = 0; j + 1 < pp && kind != 3; ++j) {
     int th;
     if (kind == 0) {
       if (j >= pp - 2) break;

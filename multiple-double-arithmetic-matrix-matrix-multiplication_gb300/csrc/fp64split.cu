@@ -9,8 +9,11 @@
 // DMMAs run over the same chunks (k, j0..j0+3), k outer, j0 inner, with the
 // same four operands per chunk, and the chunks whose B part is zero for the
 // whole tile (j0 > i) are skipped, which removes half of the reference's
-// tensor work.  Slices are read from the reference's own AoS layout
-// (m x k x pp), four consecutive slices of one entry per 32-byte sector.
+// tensor work.  Operands are addressed through element strides: the
+// reference's AoS layout (m x k x pp; four consecutive slices of one entry
+// per 32-byte sector) for mdg_slice_conv, and slice planes (pp planes of
+// m x k, the layout of the CPU convolution driver TCcudant.cpp:172-276) for
+// mdg_plane_conv.
 //
 // GB300 note: FP64 tensor throughput on this part is a small fraction of its
 // BF16 rate; this kernel is the baseline the BF16 slice form is measured
@@ -26,11 +29,18 @@ __device__ __forceinline__ void dmma(double (&c)[2], double a, double b) {
       : "d"(a), "d"(b));
 }
 
+// Element (row, k, slice) of A sits at row * ar + kk * ak + j * aj, and so
+// on for B (k, column, slice) and C (row, column, slice).
+struct ConvStrides {
+  long long ar, ak, aj, bk, bc, bj, cr, cc, ci;
+};
+
 // Block: 4 warps as 2 x 2, tile 64 rows x 32 columns of diagonal i =
 // blockIdx.z.  Warp tile: 32 rows (4 m8 tiles) x 16 columns (2 n8 tiles).
 __global__ void __launch_bounds__(128)
     slice_conv_kernel(int pp, int m, int n, int k, const double *__restrict__ Aq,
-                      const double *__restrict__ Bq, double *__restrict__ Cq) {
+                      const double *__restrict__ Bq, double *__restrict__ Cq,
+                      const ConvStrides sd) {
   const int i = blockIdx.z;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane >> 2, t = lane & 3;
@@ -54,10 +64,14 @@ __global__ void __launch_bounds__(128)
       double a[4], b[2];
 #pragma unroll
       for (int mi = 0; mi < 4; ++mi)
-        a[mi] = (rows[mi] < m && ja < pp) ? __ldg(Aq + ((size_t)rows[mi] * k + kk) * pp + ja) : 0.0;
+        a[mi] = (rows[mi] < m && ja < pp)
+                    ? __ldg(Aq + rows[mi] * sd.ar + kk * sd.ak + ja * sd.aj)
+                    : 0.0;
 #pragma unroll
       for (int ni = 0; ni < 2; ++ni)
-        b[ni] = (cols[ni] < n && jb >= 0) ? __ldg(Bq + ((size_t)kk * n + cols[ni]) * pp + jb) : 0.0;
+        b[ni] = (cols[ni] < n && jb >= 0)
+                    ? __ldg(Bq + kk * sd.bk + cols[ni] * sd.bc + jb * sd.bj)
+                    : 0.0;
 #pragma unroll
       for (int mi = 0; mi < 4; ++mi)
 #pragma unroll
@@ -73,7 +87,7 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int c = col_base + ni * 8 + 2 * t + h;
-        if (c < n) Cq[((size_t)r * n + c) * pp + i] = acc[mi][ni][h];
+        if (c < n) Cq[r * sd.cr + c * sd.cc + i * sd.ci] = acc[mi][ni][h];
       }
   }
 }
@@ -83,11 +97,14 @@ __global__ void __launch_bounds__(128)
 namespace mdgi {
 
 int launch_slice_conv(int pp, int m, int n, int k, const double *Aq, const double *Bq,
-                      double *Cq, cudaStream_t st) {
+                      double *Cq, int planes, cudaStream_t st) {
   if (m == 0 || n == 0 || pp == 0) return MDG_SUCCESS;
   if (pp > 65535) return MDG_ERROR_INVALID_SIZE;
+  const long long P = pp, M = m, N = n, K = k;
+  const ConvStrides aos{K * P, P, 1, N * P, P, 1, N * P, P, 1};
+  const ConvStrides soa{K, 1, M * K, N, 1, K * N, N, 1, M * N};
   dim3 grid(ceil_div(n, 32), ceil_div(m, 64), pp);
-  slice_conv_kernel<<<grid, 128, 0, st>>>(pp, m, n, k, Aq, Bq, Cq);
+  slice_conv_kernel<<<grid, 128, 0, st>>>(pp, m, n, k, Aq, Bq, Cq, planes ? soa : aos);
   MDG_TRY_LAUNCH();
   return MDG_SUCCESS;
 }

@@ -69,6 +69,8 @@ def lib():
         L.orc_gemm_slices.argtypes = [ctypes.c_int] * 6 + [_dp, _dp, _dp]
         L.orc_has_openmp.restype = ctypes.c_int
         L.orc_plane_conv.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
+        L.orc_generate.argtypes = [ctypes.c_int] * 4 + [ctypes.c_uint64, ctypes.c_int,
+                                                        ctypes.c_int, _dp]
         _lib = L
     return _lib
 
@@ -183,6 +185,14 @@ def plane_conv(n, pp, A, B):
     C = np.zeros((pp, n, n), dtype=np.float64)
     lib().orc_plane_conv(n, pp, _ptr(A), _ptr(B), _ptr(C))
     return C
+
+
+def generate(dist, P, rows, cols, seed, e0=0, e1=0):
+    """rows x cols x P float64 from the counter-based generator (dist as in
+    mdg_generate: 0 uniform, 1 normal, 2 reference family, +4 / +8 scales)."""
+    X = np.empty((rows, cols, P), dtype=np.float64)
+    lib().orc_generate(dist, P, rows, cols, int(seed) & (2 ** 64 - 1), e0, e1, _ptr(X))
+    return X
 
 
 def has_openmp():

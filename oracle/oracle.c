@@ -22,6 +22,9 @@
  *   8. slice-digit form             the tensor-core form of this library:
  *                                   exact integer digits, exact diagonal
  *                                   sums, rounding back to P limbs
+ *   9. input generator              this library's counter-based generator
+ *                                   (mdg_generate); its reference family is
+ *                                   random_pd, floatybits.cu:107-120
  */
 #include <math.h>
 #include <stdint.h>
@@ -886,6 +889,80 @@ void orc_gemm_slices(int P, int s, int D, int m, int n, int k,
   free(dA);
   free(dB);
   free(Cd);
+}
+
+/* ------------------------------------------------------------------ 9 -- */
+
+/* splitmix64 finaliser (Vigna), the only source of randomness. */
+static uint64_t gen_mix(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+/* Word j of the stream with base b (streams: one per entry, row, column). */
+static uint64_t gen_word(uint64_t key, uint64_t index, int j) {
+  const uint64_t b = gen_mix(key ^ (index * 0xd1342543de82ef95ull));
+  return gen_mix(b + (uint64_t)(j + 1) * 0x9e3779b97f4a7c15ull);
+}
+
+static double gen_unit(uint64_t w) { /* (k - 2^52) 2^-52, k the top 53 bits */
+  return ldexp((double)((int64_t)(w >> 11) - ((int64_t)1 << 52)), -52);
+}
+
+/* dist: 0 uniform, 1 normal (Irwin-Hall of 12), 2 random_pd family; +4 row
+ * scales, +8 column scales 2^U{e0..e1}.  X is rows x cols x P, dense. */
+void orc_generate(int dist, int P, int rows, int cols, uint64_t seed, int e0, int e1,
+                  double *X) {
+  const uint64_t key = gen_mix(seed);
+  const uint64_t ke = gen_mix(key ^ 0x5851f42d4c957f2dull);
+  const uint64_t kr = gen_mix(key ^ 0xa0761d6478bd642full);
+  const uint64_t kc = gen_mix(key ^ 0xe7037ed1a0b428dbull);
+  const int kind = dist & 3;
+  for (int r = 0; r < rows; ++r)
+    for (int c = 0; c < cols; ++c) {
+      const uint64_t e = (uint64_t)r * (uint64_t)cols + (uint64_t)c;
+      double *x = X + e * (uint64_t)P;
+      if (kind == 2) {
+        int ex = e0;
+        if (e1 != e0) ex += (int)(gen_word(ke, e, 0) % (uint64_t)(e1 - e0));
+        for (int i = 0; i < P; ++i) {
+          const uint64_t f = ((uint64_t)1 << 51) | (gen_word(ke, e, 1 + i) >> 13);
+          x[i] = ldexp((double)f, ex - 52 * i - 52);
+        }
+        continue;
+      }
+      int j = 0;
+      if (kind == 1) {
+        int64_t t = -((int64_t)6 << 53);
+        for (; j < 12; ++j) t += (int64_t)(gen_word(ke, e, j) >> 11);
+        x[0] = ldexp((double)t, -53);
+      } else {
+        x[0] = gen_unit(gen_word(ke, e, j++));
+      }
+      for (int i = 1; i < P; ++i) {
+        const double ulp = x[i - 1] == 0.0 ? 0.0 : ldexp(1.0, ilogb(x[i - 1]) - 52);
+        x[i] = gen_unit(gen_word(ke, e, j + i - 1)) * ulp * 0.5;
+      }
+      for (int i = P - 2; i >= 0; --i) {
+        double err;
+        const double s = qts(x[i], x[i + 1], &err);
+        x[i] = s;
+        x[i + 1] = err;
+      }
+      for (int i = 0; i < P - 1; ++i) {
+        double err;
+        const double s = qts(x[i], x[i + 1], &err);
+        x[i] = s;
+        x[i + 1] = err;
+      }
+      int sc = 0;
+      if (dist & 4) sc += e0 + (int)(gen_word(kr, (uint64_t)r, 0) % (uint64_t)(e1 - e0 + 1));
+      if (dist & 8) sc += e0 + (int)(gen_word(kc, (uint64_t)c, 0) % (uint64_t)(e1 - e0 + 1));
+      if (sc)
+        for (int i = 0; i < P; ++i) x[i] = ldexp(x[i], sc);
+    }
 }
 
 int orc_has_openmp(void) {
