@@ -271,19 +271,35 @@ def bench_batched(api, inputs, stream):
     ops = inputs.batched_operands(probs, rng)
     dev_ops = [(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()) for A, B in ops]
     flops = sum(2.0 * m * n * k for _, m, n, k in probs)
-    plan = api.BatchPlan(dev_ops)
-    plan.run()
-    torch.cuda.synchronize()
-    g = torch.cuda.CUDAGraph()
-    s = torch.cuda.Stream()
-    s.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(s):
-        with torch.cuda.graph(g, stream=s):
-            plan.run(stream=s)
-    for _ in range(3):
-        g.replay()
-    torch.cuda.synchronize()
+    def captured(pairs):
+        plan = api.BatchPlan(pairs)
+        plan.run()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                plan.run(stream=s)
+        for _ in range(3):
+            g.replay()
+        torch.cuda.synchronize()
+        return plan, g
+
+    plan, g = captured(dev_ops)
     t_graph = event_time(g.replay, torch.cuda.current_stream(), iters=5)
+    # the metric per P (each P's problems as their own graph-replayed plan)
+    per_p = {}
+    for P in (2, 4, 8):
+        sel = [i for i, pr in enumerate(probs) if pr[0] == P]
+        if not sel:
+            continue
+        _, gp = captured([dev_ops[i] for i in sel])
+        tp = event_time(gp.replay, torch.cuda.current_stream(), iters=3)
+        fp = sum(2.0 * probs[i][1] * probs[i][2] * probs[i][3] for i in sel)
+        per_p[f"p{P}"] = {"problems": len(sel), "md_gflop": fp / 1e9,
+                          "slice_graph_gflops": fp / tp / 1e9, "ms": tp * 1e3}
+        del gp
     # every C of the graph equals the single-problem slice GEMM
     same = all(torch.equal(C, api.gemm(A, B, "slice_bf16")) for (A, B), C in
                list(zip(dev_ops, plan.Cs))[:16])
@@ -300,6 +316,7 @@ def bench_batched(api, inputs, stream):
     return {"workload": "256 problems, m,n,k ~ U{32..512 step 32}, P ~ U{2,4,8}, seed 3",
             "md_gflop": flops / 1e9,
             "slice_graph_gflops": flops / t_graph / 1e9, "slice_graph_ms": t_graph * 1e3,
+            "per_p": per_p,
             "slice_launches_per_batch": 8,
             "plain_loop_gflops": flops / t_loop / 1e9, "plain_loop_ms": t_loop * 1e3,
             "plain_batched_gflops": flops / t_pb / 1e9, "plain_batched_ms": t_pb * 1e3,
@@ -435,6 +452,29 @@ def main():
                            "error_bits_normwise": round(eb[1], 1)}
         if "fp64split" in forms:
             forms["slice_over_fp64split"] = forms["slice_bf16"]["gflops"] / forms["fp64split"]["gflops"]
+        # FP64 ceiling of the two FP64 forms, measured here (the peaks file
+        # holds BF16 and HBM only): cuBLAS DGEMM through torch.matmul
+        a64 = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        torch.matmul(a64, a64)
+        t64 = event_time(lambda: torch.matmul(a64, a64), stream, iters=3)
+        fp64 = 2.0 * 4096 ** 3 / t64 / 1e12
+        del a64
+        forms["fp64_peak"] = {"tflops": fp64, "how": "torch.matmul float64 4096^3 (cuBLAS "
+                              "DGEMM), 3 launches, CUDA events"}
+        mnk = 1024.0 ** 3
+        # split form: per (row, column, k) the DMMA chunks of the 16 output
+        # slices hold sum_i 4 ceil((i + 1) / 4) = 160 multiply-adds
+        sp = 2.0 * 160 * mnk / (forms["fp64split"]["ms"] / 1e3) / 1e12
+        forms["fp64split"]["roofline"] = {"bound": "fp64 tensor (DMMA)", "achieved_tflops": sp,
+                                          "peak_tflops": fp64, "frac": sp / fp64}
+        # plain form: 425 FP64 operations per quad-double multiply-add (the
+        # reference's count, TCtest.cu:136-148), each its own instruction
+        pl = 425.0 * mnk / (forms["plain"]["ms"] / 1e3) / 1e12
+        forms["plain"]["roofline"] = {"bound": "fp64 CUDA cores", "achieved_tflops": pl,
+                                      "peak_tflops": fp64, "frac": pl / fp64,
+                                      "note": "425 FP64 operations per qd multiply-add "
+                                              "(TCtest.cu:136-148), issued as unfused mul/add, "
+                                              "against the DGEMM flop rate"}
 
     batched = None
     if not args.no_forms and rank == 0:

@@ -104,6 +104,23 @@ int mdg_gemm(int form, int p, int m, int n, int k, const double *A, int lda,
              const mdg_options *opt, void *workspace, size_t workspace_bytes,
              void *stream);
 
+/* C = op(A) op(B), or C = C (+) op(A) op(B) with accumulate = 1, where
+ * op(A) = A (m x k, lda >= k) or, with trans_a = 1, the transpose of A
+ * stored k x m (lda >= m); op(B) = B (k x n, ldb >= n) or, with trans_b = 1,
+ * the transpose of B stored n x k (ldb >= k); (+) is the reference's
+ * P-double addition (ddf_add for P = 2, else baileyAdd_fast,
+ * quad_double_functions.cu:216).  The result equals mdg_gemm of the same
+ * form on the transposed operands, then the addition; with k = 0 C is
+ * cleared (or kept, when accumulating).  Extends the reference's square,
+ * overwrite-only call (TCcuda.h:66).  Workspace: mdg_gemm_ex_workspace_size
+ * (the inner GEMM's plus transposed copies and the product when needed). */
+size_t mdg_gemm_ex_workspace_size(int form, int trans_a, int trans_b, int accumulate,
+                                  int p, int m, int n, int k, const mdg_options *opt);
+int mdg_gemm_ex(int form, int trans_a, int trans_b, int accumulate, int p, int m, int n,
+                int k, const double *A, int lda, const double *B, int ldb, double *C,
+                int ldc, const mdg_options *opt, void *workspace,
+                size_t workspace_bytes, void *stream);
+
 /* C = A * B with HOST buffers: copies in, computes, copies out, waits.
  * Device memory comes from a cache owned by the library (freed by
  * mdg_release_cache).  This is the call the std::vector wrappers make. */

@@ -38,6 +38,9 @@ SIGNATURES = {
     "mdg_gemm": (c_int, [c_int] * 5 + [c_vp, c_int, c_vp, c_int, c_vp, c_int, _P_OPT, c_vp, c_size,
                                         c_vp]),
     "mdg_gemm_host": (c_int, [c_int] * 5 + [c_vp, c_vp, c_vp, _P_OPT]),
+    "mdg_gemm_ex_workspace_size": (c_size, [c_int] * 8 + [_P_OPT]),
+    "mdg_gemm_ex": (c_int, [c_int] * 8 + [c_vp, c_int, c_vp, c_int, c_vp, c_int, _P_OPT, c_vp,
+                                          c_size, c_vp]),
     "mdg_gemm_batched_workspace_size": (c_size, [c_int, _P_PROB, c_int, _P_OPT]),
     "mdg_gemm_batched": (c_int, [c_int, _P_PROB, c_int, _P_OPT, c_vp, c_size, c_vp]),
     "mdg_release_cache": (None, []),

@@ -74,6 +74,39 @@ def gemm(A, B, form="slice_bf16", out=None, workspace=None, stream=None, **kw):
     return C
 
 
+def _ld(X, p):
+    """Leading dimension (entries) of a (rows, cols, p) view whose rows may be
+    padded: the entries of a row and the limbs of an entry must be dense."""
+    assert X.stride(2) == 1 and (X.shape[1] <= 1 or X.stride(1) == p)
+    return max(X.stride(0) // p if X.shape[0] > 1 else X.shape[1], X.shape[1], 1)
+
+
+def gemm_ex(A, B, form="slice_bf16", trans_a=False, trans_b=False, C=None, accumulate=False,
+            workspace=None, stream=None, **kw):
+    """C = op(A) op(B), or C (+)= op(A) op(B) with accumulate (the P-double
+    addition), through mdg_gemm_ex.  A is (m, k, P), or (k, m, P) with
+    trans_a; B is (k, n, P), or (n, k, P) with trans_b; views with padded
+    rows pass their row stride as the leading dimension."""
+    p = A.shape[2]
+    m, k = (A.shape[1], A.shape[0]) if trans_a else (A.shape[0], A.shape[1])
+    n = B.shape[0] if trans_b else B.shape[1]
+    assert (B.shape[1] if trans_b else B.shape[0]) == k and B.shape[2] == p
+    if C is None:
+        assert not accumulate
+        C = torch.empty((m, n, p), dtype=torch.float64, device=A.device)
+    opt = _opts(**kw)
+    f = FORMS[form]
+    need = lib().mdg_gemm_ex_workspace_size(f, int(trans_a), int(trans_b), int(accumulate), p, m,
+                                            n, k, ctypes.byref(opt))
+    if need and (workspace is None or workspace.numel() < need):
+        workspace = torch.empty(need, dtype=torch.uint8, device=A.device)
+    check(lib().mdg_gemm_ex(f, int(trans_a), int(trans_b), int(accumulate), p, m, n, k,
+                            _ptr(A), _ld(A, p), _ptr(B), _ld(B, p), _ptr(C), _ld(C, p),
+                            ctypes.byref(opt), _ptr(workspace) if need else None, need,
+                            _stream(stream)), "mdg_gemm_ex")
+    return C
+
+
 def gemm_host(A, B, form="slice_bf16", **kw):
     """C = A @ B for host numpy arrays through mdg_gemm_host (copies in and
     out inside the call)."""

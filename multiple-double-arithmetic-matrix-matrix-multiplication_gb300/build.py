@@ -25,7 +25,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler",
           "--expt-relaxed-constexpr"] + ARCH
 
 SOURCES = ["capi.cu", "plain_gemm.cu", "floatybits.cu", "fp64split.cu", "slice_tc.cu",
-           "diag_gemm_tc.cu", "dropin.cu", "noalloc.cu", "batched.cu", "generate.cu"]
+           "diag_gemm_tc.cu", "dropin.cu", "noalloc.cu", "batched.cu", "generate.cu",
+           "gemm_ex.cu"]
 
 
 def _compile(src):
