@@ -50,6 +50,13 @@ WORKLOADS = {
 }
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the paced CTA-pair diagonal GEMM, from one-pass ncu captures of the bench's
+# own command on this machine's GB300 (quad-double, seed 4 inputs):
+#   8192^3: 462.35 GB read + 17.27 GB written;  4096^3: 71.66 + 2.69 GB.
+DIAG_TRAFFIC_BYTES = {"qd8192_normal": 479.62e9, "qd4096_normal": 74.35e9}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -499,12 +506,16 @@ def main():
             "e2e": {"value": flops * world / t_e2e / 1e9, "unit": UNIT,
                     "h2d_bytes_per_step": A.nbytes + B.nbytes,
                     "d2h_bytes_per_step": m * n * P * 8,
-                    "call": "mdg_gemm_host (pinned host buffers)",
+                    "call": "mdg_gemm_host (pinned host buffers; B, then A in row panels "
+                            "overlapped with the GEMM, C panels copied back behind it)",
                     "h2d_gbs": A.nbytes / t_h2d / 1e9,
                     "pipelined_value": flops * world / pipe / 1e9,
                     "pipelined": "mdg_gemm on two device buffer sets; H2D of step i+1 and D2H of step i on copy streams overlap the GEMM of step i"},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_sust,
-                         "unit": "TFLOP/s", "frac": achieved / bf16_sust, "traffic": None,
+                         "unit": "TFLOP/s", "frac": achieved / bf16_sust,
+                         "traffic": DIAG_TRAFFIC_BYTES.get(args.workload),
+                         "traffic_note": "DRAM bytes per launch, one-pass ncu capture; the "
+                                         "operands are 2 x 3.76 GB of digit planes",
                          "kernel": "diag_gemm", "kernel_ms": t_diag * 1e3,
                          "algorithmic_tflop_per_launch": tflop,
                          "peak_kind": f"{peak_kind} bf16 sustained"},

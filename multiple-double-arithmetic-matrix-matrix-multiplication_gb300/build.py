@@ -24,9 +24,13 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler",
           "-fPIC,-ffp-contract=off", "-I", INCLUDE, "-I", CSRC,
           "--expt-relaxed-constexpr"] + ARCH
 
+# The wide-integer stage kernels are spread over one unit per limb count
+# (renorm_p*) and per integer width (batched_w*), so that ptxas works on
+# them in parallel; the longest unit then bounds the build.
 SOURCES = ["capi.cu", "plain_gemm.cu", "floatybits.cu", "fp64split.cu", "slice_tc.cu",
            "diag_gemm_tc.cu", "dropin.cu", "noalloc.cu", "batched.cu", "generate.cu",
-           "gemm_ex.cu"]
+           "gemm_ex.cu", "renorm_p2.cu", "renorm_p4.cu", "renorm_p8.cu", "renorm_p16.cu",
+           "batched_w4.cu", "batched_w6.cu", "batched_w10.cu", "batched_w16.cu"]
 
 
 def _compile(src):
@@ -46,7 +50,7 @@ def _compile(src):
 def build(verbose=False):
     os.makedirs(OBJ_DIR, exist_ok=True)
     os.makedirs(OUT_DIR, exist_ok=True)
-    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 1)) as ex:
         results = list(ex.map(_compile, SOURCES))
     objs = [o for o, _ in results]
     if verbose:

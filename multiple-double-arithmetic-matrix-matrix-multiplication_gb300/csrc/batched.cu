@@ -26,25 +26,7 @@
 #include "slice_stages.cuh"
 #include "slice_tc.cuh"
 
-namespace mdgi {
-
-struct BatchProblem {
-  int p, s, D, m, n, k, Mp, Np, Kp;
-  const double *A, *B;
-  double *C;
-  int lda, ldb, ldc;
-  int offE, offF;  // row maxima / exponents of A at offE, of B's columns at offF
-  __nv_bfloat16 *dA, *dB;
-  int *chunks;
-  long long plane_a, plane_b, plane_c;
-  int rowblk_begin;  // absmax of A: blocks of 256 rows
-  int colblk_begin;  // absmax of B: blocks of 256 rows of B (k)
-  int digA_begin;    // digits of A: rows Mp
-  int digB_begin;    // digits of B: rows Np
-  int out_begin;     // renorm: rows m
-};
-
-}  // namespace mdgi
+#include "batched_table.cuh"
 
 struct mdg_batch_s {
   int count = 0, nw = 4, total_tiles = 0;
@@ -60,21 +42,7 @@ struct mdg_batch_s {
 namespace {
 
 using mdgi::BatchProblem;
-
-template <int Field>
-__device__ __forceinline__ int find_problem(const BatchProblem *pr, int count, int x) {
-  int lo = 0, hi = count - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    const int b = Field == 0 ? pr[mid].rowblk_begin
-                  : Field == 1 ? pr[mid].colblk_begin
-                  : Field == 2 ? pr[mid].digA_begin
-                  : Field == 3 ? pr[mid].digB_begin
-                               : pr[mid].out_begin;
-    if (b <= x) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
+using mdgi::find_problem;
 
 __global__ void absmax_rows_b(const BatchProblem *__restrict__ pr, int count,
                               unsigned long long *bits) {
@@ -97,47 +65,6 @@ __global__ void absmax_cols_b(const BatchProblem *__restrict__ pr, int count,
 __global__ void exps_b(int count, const unsigned long long *__restrict__ bits, int *__restrict__ E) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count) E[i] = mdgi::scale_exp(__longlong_as_double((long long)bits[i]));
-}
-
-template <int NW, int Side>
-__global__ void digits_b(const BatchProblem *__restrict__ pr, int count, const int *__restrict__ E) {
-  const int q = find_problem<Side == 0 ? 2 : 3>(pr, count, blockIdx.x);
-  const BatchProblem &b = pr[q];
-  const int pc = blockIdx.y * blockDim.x + threadIdx.x;
-  if (pc >= b.Kp) return;
-  if (Side == 0)
-    mdgi::digits_elem<NW>(b.p, b.s, b.m, b.k, b.A, b.lda, E + b.offE, 0, b.dA, b.Kp, b.plane_a,
-                          b.Mp, b.Kp, blockIdx.x - b.digA_begin, pc);
-  else
-    mdgi::digits_elem<NW>(b.p, b.s, b.n, b.k, b.B, b.ldb, E + b.offF, 1, b.dB, b.Kp, b.plane_b,
-                          b.Np, b.Kp, blockIdx.x - b.digB_begin, pc);
-}
-
-template <int NW>
-__global__ void __launch_bounds__(128) renorm_b(const BatchProblem *__restrict__ pr, int count,
-                                                const int *__restrict__ E) {
-  const int q = find_problem<4>(pr, count, blockIdx.x);
-  const BatchProblem &b = pr[q];
-  const int r = blockIdx.x - b.out_begin, c = blockIdx.y * blockDim.x + threadIdx.x;
-  const int KB = b.Kp / 64;
-  switch (b.p) {
-    case 2:
-      mdgi::renorm_elems<2, NW, 1>(b.s, b.D, KB, b.m, b.n, b.chunks, b.plane_c, b.Np,
-                                   E + b.offE, E + b.offF, b.C, b.ldc, r, c);
-      break;
-    case 4:
-      mdgi::renorm_elems<4, NW, 1>(b.s, b.D, KB, b.m, b.n, b.chunks, b.plane_c, b.Np,
-                                   E + b.offE, E + b.offF, b.C, b.ldc, r, c);
-      break;
-    case 8:
-      mdgi::renorm_elems<8, NW, 1>(b.s, b.D, KB, b.m, b.n, b.chunks, b.plane_c, b.Np,
-                                   E + b.offE, E + b.offF, b.C, b.ldc, r, c);
-      break;
-    default:
-      mdgi::renorm_elems<16, NW, 1>(b.s, b.D, KB, b.m, b.n, b.chunks, b.plane_c, b.Np,
-                                    E + b.offE, E + b.offF, b.C, b.ldc, r, c);
-      break;
-  }
 }
 
 struct Layout {
@@ -308,13 +235,9 @@ int mdg_batch_run(mdg_batch_s *h, void *stream) {
   const dim3 gb(h->total_digB, mdgi::ceil_div(h->max_Kp, 128));
   const dim3 gr(h->total_out, mdgi::ceil_div(h->max_n, 128));
 #define MDG_BATCH_NW(W)                                                            \
-  digits_b<W, 0><<<ga, 128, 0, st>>>(h->dprobs, h->count, h->exps);                \
-  MDG_TRY_LAUNCH();                                                                \
-  digits_b<W, 1><<<gb, 128, 0, st>>>(h->dprobs, h->count, h->exps);                \
-  MDG_TRY_LAUNCH();                                                                \
+  MDG_TRY(mdgi::launch_batch_digits<W>(h->dprobs, h->count, h->exps, ga, gb, st));  \
   MDG_TRY(mdgi::launch_diag_gemm_grouped(h->dgroups, h->count, h->total_tiles, st)); \
-  renorm_b<W><<<gr, 128, 0, st>>>(h->dprobs, h->count, h->exps);                   \
-  MDG_TRY_LAUNCH();
+  MDG_TRY(mdgi::launch_batch_renorm<W>(h->dprobs, h->count, h->exps, gr, st));
   switch (h->nw) {
     case 4: MDG_BATCH_NW(4); break;
     case 6: MDG_BATCH_NW(6); break;

@@ -1,0 +1,8 @@
+// Batched digit and renormalisation kernels with 10-word integers
+// (see batched_stages.cuh).
+#include "batched_stages.cuh"
+
+template int mdgi::launch_batch_digits<10>(const mdgi::BatchProblem *, int, const int *, dim3,
+                                           dim3, cudaStream_t);
+template int mdgi::launch_batch_renorm<10>(const mdgi::BatchProblem *, int, const int *, dim3,
+                                           cudaStream_t);

@@ -43,10 +43,48 @@ int engine_choice(int opt) {
 // ------------------------------------------------------------------ cache --
 // Grow-only device buffers owned by the library, for calls that take no
 // workspace argument (mdg_gemm_host, mdg_scale_exponents).  One per slot.
+// The buffers, streams and events belong to one device; a call on another
+// device releases them first.
+constexpr int kMaxPanels = 4;
 struct DeviceCache {
   std::mutex mu;
+  int dev = -1;
   void *ptr[4] = {nullptr, nullptr, nullptr, nullptr};
   size_t cap[4] = {0, 0, 0, 0};
+  cudaStream_t streams[3] = {nullptr, nullptr, nullptr};  // compute, copies in, copies out
+  cudaEvent_t events[2 + 2 * kMaxPanels] = {};  // start, B in, A panels in, C panels done
+  // caller holds mu
+  int bind_device() {
+    int d = 0;
+    MDG_TRY_CUDA(cudaGetDevice(&d));
+    if (d != dev) {
+      release_locked();
+      dev = d;
+    }
+    return MDG_SUCCESS;
+  }
+  int make_streams() {
+    for (auto &st : streams)
+      if (!st) MDG_TRY_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    for (auto &ev : events)
+      if (!ev) MDG_TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    return MDG_SUCCESS;
+  }
+  void release_locked() {
+    for (int i = 0; i < 4; ++i) {
+      if (ptr[i]) cudaFree(ptr[i]);
+      ptr[i] = nullptr;
+      cap[i] = 0;
+    }
+    for (auto &st : streams) {
+      if (st) cudaStreamDestroy(st);
+      st = nullptr;
+    }
+    for (auto &ev : events) {
+      if (ev) cudaEventDestroy(ev);
+      ev = nullptr;
+    }
+  }
   int get(int slot, size_t bytes, void **out) {
     if (bytes == 0) bytes = 256;
     if (cap[slot] < bytes) {
@@ -65,11 +103,8 @@ struct DeviceCache {
   }
   void release() {
     std::lock_guard<std::mutex> lk(mu);
-    for (int i = 0; i < 4; ++i) {
-      if (ptr[i]) cudaFree(ptr[i]);
-      ptr[i] = nullptr;
-      cap[i] = 0;
-    }
+    release_locked();
+    dev = -1;
   }
 };
 static DeviceCache g_cache;
@@ -181,6 +216,61 @@ static size_t workspace_bytes(int form, int p, int m, int n, int k, const Opts &
 
 using namespace mdgi;
 
+// mdg_gemm_host for the BF16 form on tall problems: B is copied in and its
+// exponents and digits computed once, then A is copied in row panels on one
+// copy stream while the previous panel computes, and each finished panel of
+// C goes back on a second copy stream, so most of the host-link traffic hides
+// behind the tensor-core work.  Bits as one mdg_gemm (slice_panel).  The
+// work starts after everything queued before it on the legacy default
+// stream and the blocking streams, as the single-stream path would.
+static int host_slice_panels(int p, const Opts &o, int m, int n, int k, const double *A,
+                             const double *B, double *C, double *dA, double *dB, double *dC) {
+  const int want = std::min(kMaxPanels, m / 1024);
+  const int mp = (int)align_up((m + want - 1) / want, 256);
+  const int panels = (m + mp - 1) / mp;
+  const SlicePlan pl = make_slice_plan(p, o.slices, o.diagonals, mp, n, k);
+  if (pl.Mp > 65535 || pl.Np > 65535) return MDG_ERROR_NOT_SUPPORTED;
+  void *ws = nullptr;
+  MDG_TRY(g_cache.get(3, pl.total, &ws));
+  MDG_TRY(g_cache.make_streams());
+  cudaStream_t sc = g_cache.streams[0], si = g_cache.streams[1], so = g_cache.streams[2];
+  cudaEvent_t ev0 = g_cache.events[0], evB = g_cache.events[1];
+  cudaEvent_t *evA = g_cache.events + 2, *evC = g_cache.events + 2 + kMaxPanels;
+  const size_t row_a = sizeof(double) * (size_t)k * p, row_c = sizeof(double) * (size_t)n * p;
+  const size_t ea = (size_t)k * p, ec = (size_t)n * p;  // doubles per row
+  MDG_TRY_CUDA(cudaEventRecord(ev0, 0));
+  MDG_TRY_CUDA(cudaStreamWaitEvent(si, ev0, 0));
+  MDG_TRY_CUDA(cudaStreamWaitEvent(sc, ev0, 0));
+  MDG_TRY_CUDA(cudaMemcpyAsync(dB, B, sizeof(double) * (size_t)k * n * p, cudaMemcpyHostToDevice,
+                               si));
+  MDG_TRY_CUDA(cudaEventRecord(evB, si));
+  MDG_TRY_CUDA(cudaMemcpyAsync(dA, A, row_a * std::min(mp, m), cudaMemcpyHostToDevice, si));
+  MDG_TRY_CUDA(cudaEventRecord(evA[0], si));
+  MDG_TRY_CUDA(cudaStreamWaitEvent(sc, evB, 0));
+  MDG_TRY(slice_prepare_b(pl, dB, n, ws, sc));
+  const int engine = engine_choice(o.engine);
+  for (int i = 0; i < panels; ++i) {
+    const int r0 = i * mp, rows = std::min(mp, m - r0);
+    if (i + 1 < panels) {
+      const int r1 = r0 + mp, rows1 = std::min(mp, m - r1);
+      MDG_TRY_CUDA(cudaMemcpyAsync(dA + r1 * ea, A + r1 * ea, row_a * rows1,
+                                   cudaMemcpyHostToDevice, si));
+      MDG_TRY_CUDA(cudaEventRecord(evA[i + 1], si));
+    }
+    MDG_TRY_CUDA(cudaStreamWaitEvent(sc, evA[i], 0));
+    MDG_TRY(slice_panel(pl, rows, dA + r0 * ea, k, dC + r0 * ec, n, ws, engine, o.parts, o.raster,
+                        sc));
+    MDG_TRY_CUDA(cudaEventRecord(evC[i], sc));
+    MDG_TRY_CUDA(cudaStreamWaitEvent(so, evC[i], 0));
+    MDG_TRY_CUDA(cudaMemcpyAsync(C + r0 * ec, dC + r0 * ec, row_c * rows, cudaMemcpyDeviceToHost,
+                                 so));
+  }
+  MDG_TRY_CUDA(cudaStreamSynchronize(si));
+  MDG_TRY_CUDA(cudaStreamSynchronize(sc));
+  MDG_TRY_CUDA(cudaStreamSynchronize(so));
+  return MDG_SUCCESS;
+}
+
 extern "C" {
 
 const char *mdg_status_string(int status) {
@@ -253,12 +343,15 @@ int mdg_gemm_host(int form, int p, int m, int n, int k, const double *A, const d
   MDG_TRY(resolve_opts(p, opt, &o));
   if (m == 0 || n == 0) return MDG_SUCCESS;
   std::lock_guard<std::mutex> lk(g_cache.mu);
+  MDG_TRY(g_cache.bind_device());
   const size_t sa = sizeof(double) * (size_t)m * k * p, sb = sizeof(double) * (size_t)k * n * p,
                sc = sizeof(double) * (size_t)m * n * p;
   void *dA, *dB, *dC, *ws = nullptr;
   MDG_TRY(g_cache.get(0, sa, &dA));
   MDG_TRY(g_cache.get(1, sb, &dB));
   MDG_TRY(g_cache.get(2, sc, &dC));
+  if (form == MDG_FORM_SLICE_BF16 && k > 0 && m >= 2048)
+    return host_slice_panels(p, o, m, n, k, A, B, C, (double *)dA, (double *)dB, (double *)dC);
   const size_t need = workspace_bytes(form, p, m, n, k, o);
   if (need) MDG_TRY(g_cache.get(3, need, &ws));
   cudaStream_t st = 0;
@@ -427,6 +520,7 @@ int mdg_scale_exponents(int p, int m, int n, int k, const double *A, int lda, co
   if ((m > 0 && (!E || (k > 0 && !A))) || (n > 0 && (!F || (k > 0 && !B))))
     return MDG_ERROR_NULL_POINTER;
   std::lock_guard<std::mutex> lk(g_cache.mu);
+  MDG_TRY(g_cache.bind_device());
   void *bits;
   MDG_TRY(g_cache.get(3, sizeof(unsigned long long) * (size_t)(std::max(m, 1) + std::max(n, 1)),
                       &bits));

@@ -1,0 +1,5 @@
+// Renormalisation kernels for P = 16 (see renorm_launch.cuh).
+#include "renorm_launch.cuh"
+
+template int mdgi::launch_renorm_p<16>(int, int, int, int, int, int, int, const int *, long long,
+                                      int, const int *, const int *, double *, int, cudaStream_t);

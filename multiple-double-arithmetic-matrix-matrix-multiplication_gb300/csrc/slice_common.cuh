@@ -91,6 +91,21 @@ __device__ __forceinline__ void wide_neg(uint64_t (&w)[NW]) {
   }
 }
 
+// x = m 2^e2 with m an integer, |m| < 2^53 (0 for x = +-0), read from the
+// IEEE fields of a finite x with integer instructions only: the FP64 units
+// of this GPU are narrow, and frexp / ldexp / an FP64-to-int conversion per
+// limb kept them 80 % busy in the digit split.  Normal x: m = +-(fraction +
+// 2^52), e2 = biased exponent - 1075; subnormal x: m = +-fraction,
+// e2 = -1074.  m 2^e2 equals x exactly, so floor(x 2^q) is unchanged.
+__device__ __forceinline__ int64_t exact_significand(double x, int &e2) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const int be = (int)((b >> 52) & 0x7ff);
+  const int64_t frac = (int64_t)(b & 0xfffffffffffffull);
+  const int64_t mag = be ? (frac | (1ll << 52)) : frac;
+  e2 = (be ? be : 1) - 1075;
+  return (b >> 63) ? -mag : mag;
+}
+
 // Scale exponent of a row / column from the largest sum of absolute limbs
 // M: the frexp exponent of M, plus one when M lies within 2^-29 of 2^e.
 __device__ __forceinline__ int scale_exp(double M) {

@@ -66,12 +66,10 @@ __device__ __forceinline__ void digits_elem(int P, int s, int rows, int cols,
 #pragma unroll
   for (int i = 0; i < NW; ++i) w[i] = 0;
   for (int l = 0; l < P; ++l) {
-    const double x = a[l];
-    if (x == 0.0) continue;
-    int e;
-    const double f = frexp(x, &e);
-    const int64_t m = (int64_t)ldexp(f, 53);
-    const int q = e - 53 + S - Er;
+    int e2;
+    const int64_t m = mdgi::exact_significand(a[l], e2);
+    if (m == 0) continue;
+    const int q = e2 + S - Er;
     if (q >= 0) {
       mdgi::wide_add_shifted<NW>(w, m, q);
     } else if (q > -64) {
@@ -130,12 +128,10 @@ __device__ __forceinline__ void digits_elem4(int P, int s, int rows, int cols,
     const int pc = pc0 + e;
     const double *a = trans ? X + ((size_t)pc * ldx + pr) * P : X + ((size_t)pr * ldx + pc) * P;
     for (int l = 0; l < P; ++l) {
-      const double x = pc < cols ? a[l] : 0.0;
-      if (x == 0.0) continue;
-      int ex;
-      const double f = frexp(x, &ex);
-      const int64_t m = (int64_t)ldexp(f, 53);
-      const int q = ex - 53 + S - Er;
+      int e2;
+      const int64_t m = pc < cols ? mdgi::exact_significand(a[l], e2) : 0;
+      if (m == 0) continue;
+      const int q = e2 + S - Er;
       if (q >= 0) {
         mdgi::wide_add_shifted<NW>(w[e], m, q);
       } else if (q > -64) {

@@ -193,16 +193,6 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// --------------------------------------------------------------- renorm --
-template <int P, int NW, int V>
-__global__ void __launch_bounds__(128)
-    renorm_kernel(int s, int D, int KB, int m, int n, const int *__restrict__ chunks,
-                  long long plane_c, int ldcd, const int *__restrict__ E,
-                  const int *__restrict__ F, double *__restrict__ C, int ldc) {
-  mdgi::renorm_elems<P, NW, V>(s, D, KB, m, n, chunks, plane_c, ldcd, E, F, C, ldc, blockIdx.y,
-                               (blockIdx.x * blockDim.x + threadIdx.x) * V);
-}
-
 }  // namespace
 
 namespace mdgi {
@@ -339,36 +329,59 @@ int launch_renorm(int p, int s, int D, int KB, int m, int n, const int *chunks,
   while (V > 1 && ((ldcd % V) || (plane_c % V) ||
                    (reinterpret_cast<uintptr_t>(chunks) % (4 * V))))
     V >>= 1;
-#define MDG_RENORM(PP, W, VV)                                                              \
-  renorm_kernel<PP, W, VV><<<dim3(ceil_div(ceil_div(n, VV), 128), m), 128, 0, st>>>(      \
-      s, D, KB, m, n, chunks, plane_c, ldcd, E, F, C, ldc)
-#define MDG_RENORM_V(PP, W)          \
-  if (V == 4 && W <= 6) {            \
-    MDG_RENORM(PP, W, 4);            \
-  } else if (V >= 2 && W <= 10) {    \
-    MDG_RENORM(PP, W, 2);            \
-  } else {                           \
-    MDG_RENORM(PP, W, 1);            \
-  }
-#define MDG_RENORM_P(PP)                    \
-  switch (NW) {                             \
-    case 4: MDG_RENORM_V(PP, 4); break;     \
-    case 6: MDG_RENORM_V(PP, 6); break;     \
-    case 10: MDG_RENORM_V(PP, 10); break;   \
-    default: MDG_RENORM_V(PP, 16); break;   \
-  }
   switch (p) {
-    case 2: MDG_RENORM_P(2); break;
-    case 4: MDG_RENORM_P(4); break;
-    case 8: MDG_RENORM_P(8); break;
-    case 16: MDG_RENORM_P(16); break;
-    default: return MDG_ERROR_INVALID_LIMBS;
+    case 2:
+      return launch_renorm_p<2>(NW, V, s, D, KB, m, n, chunks, plane_c, ldcd, E, F, C, ldc, st);
+    case 4:
+      return launch_renorm_p<4>(NW, V, s, D, KB, m, n, chunks, plane_c, ldcd, E, F, C, ldc, st);
+    case 8:
+      return launch_renorm_p<8>(NW, V, s, D, KB, m, n, chunks, plane_c, ldcd, E, F, C, ldc, st);
+    case 16:
+      return launch_renorm_p<16>(NW, V, s, D, KB, m, n, chunks, plane_c, ldcd, E, F, C, ldc, st);
+    default:
+      return MDG_ERROR_INVALID_LIMBS;
   }
-#undef MDG_RENORM_P
-#undef MDG_RENORM_V
-#undef MDG_RENORM
-  MDG_TRY_LAUNCH();
-  return MDG_SUCCESS;
+}
+
+int slice_prepare_b(const SlicePlan &pl, const double *B, int ldb, void *ws, cudaStream_t st) {
+  char *base = reinterpret_cast<char *>(ws);
+  auto *rowbits = reinterpret_cast<unsigned long long *>(base + pl.off_rowbits);
+  auto *colbits = reinterpret_cast<unsigned long long *>(base + pl.off_colbits);
+  int *E = reinterpret_cast<int *>(base + pl.off_E);
+  int *F = reinterpret_cast<int *>(base + pl.off_F);
+  MDG_TRY(launch_scale_exponents(pl.p, 0, pl.n, pl.k, nullptr, 1, B, ldb, rowbits, colbits, E, F,
+                                 st));
+  return launch_digits(pl.p, pl.s, pl.n, pl.k, B, ldb, F, 1, base + pl.off_dB, pl.Kp,
+                       pl.plane_b, pl.Np, pl.Kp, st);
+}
+
+int slice_panel(const SlicePlan &pl, int rows, const double *A, int lda, double *C, int ldc,
+                void *ws, int engine, int parts, int raster, cudaStream_t st) {
+  if (rows <= 0) return MDG_SUCCESS;
+  if (rows > pl.m) return MDG_ERROR_INVALID_SIZE;
+  char *base = reinterpret_cast<char *>(ws);
+  auto *rowbits = reinterpret_cast<unsigned long long *>(base + pl.off_rowbits);
+  auto *colbits = reinterpret_cast<unsigned long long *>(base + pl.off_colbits);
+  int *E = reinterpret_cast<int *>(base + pl.off_E);
+  int *F = reinterpret_cast<int *>(base + pl.off_F);
+  void *dA = base + pl.off_dA;
+  void *dB = base + pl.off_dB;
+  auto *Cd = reinterpret_cast<int *>(base + pl.off_Cd);
+  // E only (n = 0 leaves F, computed by slice_prepare_b, alone)
+  MDG_TRY(launch_scale_exponents(pl.p, rows, 0, pl.k, A, lda, nullptr, 1, rowbits, colbits, E,
+                                 F, st));
+  // rows beyond `rows` up to the plan's padded Mp get zero digits
+  MDG_TRY(launch_digits(pl.p, pl.s, rows, pl.k, A, lda, E, 0, dA, pl.Kp, pl.plane_a, pl.Mp,
+                        pl.Kp, st));
+  if (engine != 0) {
+    MDG_TRY(launch_diag_gemm_tc(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
+                                pl.plane_b, Cd, pl.plane_c, engine == 2 ? 1 : 0, parts, raster, st));
+  } else {
+    MDG_TRY(launch_diag_gemm_v0(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
+                                pl.plane_b, Cd, pl.plane_c, st));
+  }
+  return launch_renorm(pl.p, pl.s, pl.D, pl.Kp / 64, rows, pl.n, Cd, pl.plane_c, pl.Np, E, F, C,
+                       ldc, st);
 }
 
 int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *B, int ldb,

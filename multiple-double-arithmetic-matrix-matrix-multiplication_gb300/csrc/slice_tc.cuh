@@ -60,6 +60,12 @@ int launch_diag_gemm_v0(int s, int D, int Mp, int Np, int Kp, const void *dA, co
 int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, const void *dB,
                         int ld, long long plane_a, long long plane_b, int *chunks,
                         long long plane_c, int single, int parts, int raster, cudaStream_t st);
+// Renormalisation for P limbs with NW-word integers, V columns per thread
+// (instantiated in renorm_p{2,4,8,16}.cu).
+template <int P>
+int launch_renorm_p(int NW, int V, int s, int D, int KB, int m, int n, const int *chunks,
+                    long long plane_c, int ldcd, const int *E, const int *F, double *C, int ldc,
+                    cudaStream_t st);
 int launch_renorm(int p, int s, int D, int KB, int m, int n, const int *chunks,
                   long long plane_c, int ldcd, const int *E, const int *F, double *C, int ldc,
                   cudaStream_t st);
@@ -86,6 +92,15 @@ int tc_device_status();
 int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *B, int ldb,
                    double *C, int ldc, void *ws, int engine, int parts, int raster,
                    cudaStream_t st);
+
+// run_slice_gemm in two parts, for callers that split A into row panels
+// (the pipelined host path): slice_prepare_b computes the column exponents
+// and digits of B once; slice_panel then computes rows (<= pl.m) rows of C
+// from the matching rows of A.  Every row of C depends only on its row of A
+// and on all of B, so panels give the bits of one run_slice_gemm.
+int slice_prepare_b(const SlicePlan &pl, const double *B, int ldb, void *ws, cudaStream_t st);
+int slice_panel(const SlicePlan &pl, int rows, const double *A, int lda, double *C, int ldc,
+                void *ws, int engine, int parts, int raster, cudaStream_t st);
 
 // Which engine mdg_gemm uses for the BF16 form (MDG_SLICE_ENGINE=0/1 overrides).
 int default_engine();

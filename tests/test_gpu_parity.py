@@ -298,6 +298,19 @@ def test_host_entry_matches_device_entry(api, inputs):
         assert np.array_equal(dC, hC), form
 
 
+@pytest.mark.parametrize("m,n,k", [(2600, 300, 200), (4500, 130, 70)])
+def test_pipelined_host_entry_matches_device_entry(api, inputs, m, n, k):
+    """mdg_gemm_host of the BF16 form on m >= 2048 rows copies A in row
+    panels overlapped with the computation (2 panels of 1536 + 1064 rows,
+    4 panels of 3 x 1280 + 660): the bits equal one device-side mdg_gemm.
+    Run twice so the second call reuses the library's buffers and streams."""
+    P, A, B = inputs.workload("qd1024", m, n, k)
+    dC = host(api.gemm(dev(A), dev(B), "slice_bf16"))
+    for _ in range(2):
+        assert np.array_equal(api.gemm_host(A, B, "slice_bf16"), dC)
+    assert api.device_status() == 0
+
+
 def test_strided_operands(api, orc, inputs):
     """Leading dimensions larger than the logical sizes (views of a wider
     buffer) through the C ABI."""
