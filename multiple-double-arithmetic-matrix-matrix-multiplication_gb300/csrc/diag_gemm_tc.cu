@@ -551,7 +551,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
     diag_gemm_tc2_kernel(const __grid_constant__ CUtensorMap tmA,
                          const __grid_constant__ CUtensorMap tmB, int s, int D, int Mp, int Np,
                          int KB, int *__restrict__ out, long long plane_c, int parts,
-                         int raster, int pace, uint32_t epoch) {
+                         int raster, int pace, uint32_t epoch, int no_loads) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -653,7 +653,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
       uint32_t issued = 0, last_par = 0;
       bool pacing = pacer;
       uint32_t steps = 0;  // k-steps issued by this cluster
-      for (int u = cid; u < units; u += ncl) {
+      // no_loads (self-test of the bounded waits): issue no copy, so the
+      // MMA thread's wait for data runs out, it raises the abort flag and
+      // every role leaves with nothing in flight
+      for (int u = no_loads ? units : cid; u < units; u += ncl) {
         int tile, d0, d1;
         unit_range(u, tile, d0, d1);
         int rb, cb;
@@ -929,8 +932,14 @@ int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, co
     static std::atomic<uint32_t> epochs{0};
     uint32_t epoch = ++epochs;
     if (epoch == 0) epoch = ++epochs;
+    // MDG_TC_SELFTEST_NO_LOADS=1: the producers issue no copies, the waits
+    // for data run out after their 2 s limit and mdg_device_status then
+    // reports MDG_ERROR_TIMEOUT (a test of the failure path; the result
+    // planes are not written)
+    const char *nl = std::getenv("MDG_TC_SELFTEST_NO_LOADS");
+    const int no_loads = (nl && *nl == '1') ? 1 : 0;
     diag_gemm_tc2_kernel<<<2 * clusters, THREADS2, SMEM2_BYTES, st>>>(
-        ma, mb, s, D, Mp, Np, Kp / TK, chunks, plane_c, parts, raster, pace, epoch);
+        ma, mb, s, D, Mp, Np, Kp / TK, chunks, plane_c, parts, raster, pace, epoch, no_loads);
   } else {
     const int tiles = (Mp / TM) * (Np / TN);
     const int grid = tiles < sms ? tiles : sms;

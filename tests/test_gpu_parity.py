@@ -267,6 +267,28 @@ def test_slice_gemm_schedules_bit_identical(api, inputs, monkeypatch):
     assert api.device_status() == 0
 
 
+def test_bounded_wait_timeout_is_reported_and_context_survives(api, orc, inputs, monkeypatch):
+    """Failure path of the CTA-pair kernel without a fault: with
+    MDG_TC_SELFTEST_NO_LOADS=1 its producers issue no copies, so the MMA
+    thread's wait for data runs out after its 2 s limit; the kernel raises
+    its abort flag, every role leaves with nothing in flight and TMEM is
+    freed.  The host reads MDG_ERROR_TIMEOUT (8), and the next launch in
+    the same context computes the exact result."""
+    P, m, n, k = 4, 256, 256, 128
+    rng = np.random.default_rng(256)
+    A = inputs.uniform_pd(rng, (m, k), P)
+    B = inputs.uniform_pd(rng, (k, n), P)
+    dA, dB = dev(A), dev(B)
+    monkeypatch.setenv("MDG_TC_SELFTEST_NO_LOADS", "1")
+    api.gemm(dA, dB, "slice_bf16", engine="tc_pair")
+    assert api.device_status() == 8
+    monkeypatch.delenv("MDG_TC_SELFTEST_NO_LOADS")
+    s = api.default_slices(P)
+    got = host(api.gemm(dA, dB, "slice_bf16", engine="tc_pair"))
+    assert api.device_status() == 0
+    assert np.array_equal(got, orc.gemm_slices(P, s, s, A, B, m, n, k))
+
+
 def test_slice_gemm_hexa_double_bit_exact(api, orc, inputs):
     """P = 16 through the BF16 form (108 digits, 5886 digit pairs)."""
     rng = np.random.default_rng(16)
