@@ -435,10 +435,36 @@ def main():
     pipe = pipelined_e2e(api, hA, hB, hC, P, m, n, k, need, steps=max(2, min(args.steps, 3)))
 
     # ---- error bits on a sampled block against the exact product
-    import oracle.exact as ex
+    ex = importlib.import_module(PKG + ".errors")
     rows, cols = range(0, m, max(1, m // 6)), range(0, n, max(1, n // 6))
     C_tc = dC.cpu().numpy()
     bits = {"slice_bf16": ex.error_bits(C_tc, A, B, rows, cols)}
+    # and over a 512 x 512 block at full k against an octo-double referee:
+    # the plain form at P = 8 (the reference's matmulodf arithmetic, bit for
+    # bit, about 420 bits accurate) on the inputs zero-padded to 8 limbs
+    block_bits = None
+    if P < 8 and rank == 0:
+        R, Cn = min(512, m), min(512, n)
+        A8 = torch.zeros((R, k, 8), dtype=torch.float64, device="cuda")
+        B8 = torch.zeros((k, Cn, 8), dtype=torch.float64, device="cuda")
+        A8[..., :P] = dA[:R]
+        B8[..., :P] = dB[:, :Cn]
+        t0 = time.perf_counter()
+        ref8 = api.gemm(A8, B8, "plain")
+        torch.cuda.synchronize()
+        t_ref = time.perf_counter() - t0
+        norms = (dA[:R, :, 0].abs() @ dB[:, :Cn, 0].abs()).cpu().numpy()
+        ref8h = ref8.cpu().numpy()
+        eb = ex.referee_error_bits(C_tc[:R, :Cn], ref8h, norms)
+        # the plain form (the reference's own arithmetic) on the same block
+        plain_blk = api.gemm(dA[:R].contiguous(), dB[:, :Cn].contiguous(), "plain").cpu().numpy()
+        ep = ex.referee_error_bits(plain_blk, ref8h, norms)
+        block_bits = {"entrywise": round(eb[0], 1), "normwise": round(eb[1], 1),
+                      "plain_entrywise": round(ep[0], 1), "plain_normwise": round(ep[1], 1),
+                      "block": f"{R}x{Cn} (rows and columns from 0) at k={k}",
+                      "referee": "octo-double plain GEMM (matmulodf arithmetic) of the "
+                                 "zero-padded inputs", "referee_s": round(t_ref, 2)}
+        del A8, B8, ref8
 
     forms = None
     if not args.no_forms and rank == 0:
@@ -522,7 +548,8 @@ def main():
             "gpu_launches": 8 * args.steps,
             "clocks": clk,
             "error_bits": {"slice_bf16": [round(x, 1) for x in bits["slice_bf16"]],
-                           "sample": f"{len(rows)}x{len(cols)} entries, exact integer product"},
+                           "sample": f"{len(rows)}x{len(cols)} entries, exact integer product",
+                           "block": block_bits},
             "cpu_baseline": cpu,
             "forms": forms,
             "batched": batched,

@@ -1,10 +1,13 @@
-"""Exact products of multi-double matrices with Python integers.
+"""Error bits of computed multi-double matrices: the measurement half of the
+error reporting (not on the GEMM path; the benchmark and the tests use it).
 
-TEST INFRASTRUCTURE ONLY.  Each p-double is a finite sum of doubles, hence a
-dyadic rational; scaled by a common power of two it becomes an integer, and
-the dot products of such integers are exact.  This is the referee for the
-error bits of every GEMM form, independent of any floating-point arithmetic
-(the hexa-double GEMM of oracle.c is the second, slower referee).
+Each p-double is a finite sum of doubles, hence a dyadic rational; scaled by
+a common power of two it becomes an integer, and the dot products of such
+integers are exact.  ``error_bits`` compares a computed block of C with that
+exact product (Python integers: a few dozen entries at k = 8192).
+``referee_error_bits`` compares a large block with a higher-precision
+referee result instead (e.g. the octo-double plain GEMM of quad-double
+inputs, 2^-420 accurate), exactly, entry by entry.
 """
 import math
 
@@ -13,8 +16,8 @@ import numpy as np
 _SHIFT = 1100  # every limb here lies above 2^-1100
 
 
-def _to_int(x):
-    """sum of the limbs of x (1-D array of doubles) times 2^_SHIFT."""
+def _limbs_to_int(x, shift):
+    """sum of the limbs of x times 2^shift, exact for limbs above 2^-shift."""
     s = 0
     for v in x:
         v = float(v)
@@ -22,9 +25,15 @@ def _to_int(x):
             continue
         m, e = math.frexp(v)
         mi = int(m * (1 << 53))
-        sh = e - 53 + _SHIFT
-        s += mi << sh if sh >= 0 else mi >> (-sh)  # exact for limbs > 2^-1047
+        sh = e - 53 + shift
+        s += mi << sh if sh >= 0 else mi >> (-sh)
     return s
+
+
+
+def _to_int(x):
+    """sum of the limbs of x (1-D array of doubles) times 2^_SHIFT."""
+    return _limbs_to_int(x, _SHIFT)
 
 
 def to_ints(M):
@@ -80,5 +89,26 @@ def error_bits(Cmd, A, B, rows, cols):
             if O[a][b] != 0:
                 worst_e = max(worst_e, _log2_ratio(diff, O[a][b]))
             worst_n = max(worst_n, _log2_ratio(diff, N[a][b]))
+    cap = lambda v: 1100.0 if v == -math.inf else min(1100.0, -v)
+    return cap(worst_e), cap(worst_n)
+
+
+def referee_error_bits(C, R, N):
+    """(entrywise, normwise) error bits of C (r x c x P) against a referee R
+    (r x c x P', more precise) with N (r x c) = sum_k |a||b| per entry:
+    -log2 max |C - R| / |R| and -log2 max |C - R| / N, the differences taken
+    exactly.  Capped at 1100 for identical values."""
+    worst_e, worst_n = -math.inf, -math.inf
+    for i in range(C.shape[0]):
+        for j in range(C.shape[1]):
+            r = _limbs_to_int(R[i, j], _SHIFT)
+            d = _limbs_to_int(C[i, j], _SHIFT) - r
+            if d == 0:
+                continue
+            if r != 0:
+                worst_e = max(worst_e, _log2_ratio(d, r))
+            n = float(N[i, j])
+            if n > 0:
+                worst_n = max(worst_n, math.log2(abs(d)) - _SHIFT - math.log2(n))
     cap = lambda v: 1100.0 if v == -math.inf else min(1100.0, -v)
     return cap(worst_e), cap(worst_n)

@@ -147,7 +147,7 @@ def test_slice_conv_against_oracle(api, orc, inputs, pp, shape):
 
 @pytest.mark.parametrize("name,P", [("dd64", 2), ("qd1024", 4)])
 def test_fp64split_error_bits(api, orc, inputs, name, P):
-    import oracle.exact as ex
+    ex = pkg("errors")
     _, A, B = inputs.workload(name, 24, 24, 24)
     C = host(api.gemm(dev(A), dev(B), "fp64split"))
     ref = orc.gemm_fp64split(P, A, B, 24, 24, 24)
@@ -301,7 +301,7 @@ def test_slice_gemm_hexa_double_bit_exact(api, orc, inputs):
 
 @pytest.mark.parametrize("name", ["dd64", "qd1024", "od2048_spread"])
 def test_slice_error_bits_not_worse_than_plain(api, orc, inputs, name):
-    import oracle.exact as ex
+    ex = pkg("errors")
     P, A, B = inputs.workload(name, 48, 48, 96)
     Cs = host(api.gemm(dev(A), dev(B), "slice_bf16"))
     Cp = host(api.gemm(dev(A), dev(B), "plain"))
@@ -310,6 +310,23 @@ def test_slice_error_bits_not_worse_than_plain(api, orc, inputs, name):
     ep = ex.error_bits(Cp, A, B, rows, cols)
     print(name, "slice", es, "plain", ep)
     assert es[1] >= ep[1] - 1.0
+
+
+def test_octo_double_referee_agrees_with_exact_product(api, inputs):
+    """The benchmark's large-block error bits use the octo-double plain GEMM
+    of zero-padded quad-double inputs as referee; on a block small enough
+    for the exact integer product both measurements agree within a bit."""
+    ex = pkg("errors")
+    P, A, B = inputs.workload("qd8192_normal", 24, 20, 256)
+    C = host(api.gemm(dev(A), dev(B), "slice_bf16"))
+    A8 = np.zeros(A.shape[:2] + (8,)); A8[..., :P] = A
+    B8 = np.zeros(B.shape[:2] + (8,)); B8[..., :P] = B
+    R = host(api.gemm(dev(A8), dev(B8), "plain"))
+    norms = np.abs(A[..., 0]) @ np.abs(B[..., 0])
+    exact = ex.error_bits(C, A, B, range(24), range(20))
+    ref = ex.referee_error_bits(C, R, norms)
+    assert abs(ref[0] - exact[0]) <= 1.0 and abs(ref[1] - exact[1]) <= 1.0, (ref, exact)
+    assert ref[1] > 200
 
 
 def test_host_entry_matches_device_entry(api, inputs):

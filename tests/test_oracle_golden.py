@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, pkg
 
 
 def load(name):
@@ -97,7 +97,7 @@ def test_bigB2_layout(orc):
 def test_slice_digit_form_is_exact_on_small_case(orc, inputs):
     """Slice digits reconstruct the inputs and the diagonal GEMM keeps
     enough bits: qd 16^3 agrees with the exact product to > 212 bits."""
-    import oracle.exact as ex
+    ex = pkg("errors")
     P, A, B = inputs.workload("qd1024", 16, 16, 16)
     C = orc.gemm_slices(P, 28, 28, A, B, 16, 16, 16)
     ent, nrm = ex.error_bits(C, A, B, range(16), range(16))
