@@ -143,6 +143,28 @@ int plan_batch(const mdg_problem *problems, int count, Layout *L, mdg_batch_s *h
     h->max_n = std::max(h->max_n, q.n);
     h->max_Kp = std::max(h->max_Kp, Kp);
   }
+  if (ws) {
+    // The grouped kernel deals tiles to CTAs round-robin in table order.
+    // Heaviest tiles first (digit pairs x k-steps per tile: a quad-double
+    // tile carries ~4x the work of a double-double one, an octo-double
+    // tile ~15x), so that the deal approximates longest-processing-time-
+    // first and the CTAs finish together.  Only the order of the tiles
+    // changes; each still writes its own problem's chunk planes.
+    auto work = [](const mdgi::GroupedProblem &g) {
+      long long pairs = 0;
+      for (int d = 0; d < g.D; ++d) pairs += mdgi::diag_pairs(d, g.s);
+      return pairs * g.KB;
+    };
+    std::stable_sort(hg->begin(), hg->end(),
+                     [&](const mdgi::GroupedProblem &a, const mdgi::GroupedProblem &b) {
+                       return work(a) > work(b);
+                     });
+    int t = 0;
+    for (auto &g : *hg) {
+      g.tile_begin = t;
+      t += (g.Mp / 128) * (g.Np / 256);
+    }
+  }
   h->count = count;
   h->total_rowblk = rowblk;
   h->total_colblk = colblk;
