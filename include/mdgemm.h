@@ -254,6 +254,39 @@ int mdg_renorm_diagonals(int p, int s, int D, int k, int m, int n,
                          const int *E, const int *F, double *C, int ldc,
                          void *stream);
 
+/* ------------------------------------------------- plans and tuning -- */
+
+/* A plan for one problem shape: it owns its device workspace and the
+ * schedule it runs with.  mdg_plan_tune times the schedules that give the
+ * same bits (BF16 form: CTA pairs with diagonal ranges per tile auto / 1 /
+ * 2 / 4, and the single-CTA engine) on the caller's operands, keeps the
+ * fastest, and records it in the library's tuning cache under the device
+ * (GPU name and driver version) and the shape class (form, P, digits,
+ * padded m, n, k); plans created later for the same class start from the
+ * cached schedule.  Other forms have nothing to tune.  The cache persists
+ * as a JSON file through mdg_tune_cache_save / mdg_tune_cache_load. */
+typedef struct mdg_plan_s *mdg_plan;
+int mdg_plan_create(int form, int p, int m, int n, int k, const mdg_options *opt,
+                    mdg_plan *plan);
+size_t mdg_plan_workspace_bytes(mdg_plan plan);
+/* Runs every candidate once more after a warm-up on `stream` and waits
+ * for it; C holds the product afterwards. */
+int mdg_plan_tune(mdg_plan plan, const double *A, int lda, const double *B, int ldb,
+                  double *C, int ldc, void *stream);
+int mdg_plan_run(mdg_plan plan, const double *A, int lda, const double *B, int ldb,
+                 double *C, int ldc, void *stream);
+/* The options the plan runs with (engine, parts, raster filled in). */
+int mdg_plan_schedule(mdg_plan plan, mdg_options *out);
+void mdg_plan_destroy(mdg_plan plan);
+/* The tuning cache: {"<gpu>|<driver>": {"<form> <p> <s> <D> <Mp> <Np> <Kp>":
+ * {"engine": e, "parts": q, "raster": r, "ms": t}, ...}, ...}.  Loading
+ * merges into the cache; MDG_ERROR_NOT_SUPPORTED if the file cannot be
+ * opened, MDG_ERROR_INVALID_FORM if it is not of that form. */
+int mdg_tune_cache_load(const char *path);
+int mdg_tune_cache_save(const char *path);
+void mdg_tune_cache_clear(void);
+int mdg_tune_cache_size(void);
+
 /* ---------------------------------------------------- input generator -- */
 
 /* Distributions of mdg_generate (low two bits of dist), and scale flags

@@ -57,6 +57,16 @@ SIGNATURES = {
     "mdg_renorm_diagonals": (c_int, [c_int] * 6 + [c_vp, c_ll, c_int, c_vp, c_vp, c_vp, c_int,
                                                    c_vp]),
     "mdg_device_status": (c_int, []),
+    "mdg_plan_create": (c_int, [c_int] * 5 + [_P_OPT, ctypes.POINTER(c_vp)]),
+    "mdg_plan_workspace_bytes": (c_size, [c_vp]),
+    "mdg_plan_tune": (c_int, [c_vp, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp]),
+    "mdg_plan_run": (c_int, [c_vp, c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp]),
+    "mdg_plan_schedule": (c_int, [c_vp, _P_OPT]),
+    "mdg_plan_destroy": (None, [c_vp]),
+    "mdg_tune_cache_load": (c_int, [c_char_p]),
+    "mdg_tune_cache_save": (c_int, [c_char_p]),
+    "mdg_tune_cache_clear": (None, []),
+    "mdg_tune_cache_size": (c_int, []),
     "mdg_generate": (c_int, [c_int] * 4 + [ctypes.c_ulonglong, c_int, c_int, c_vp, c_int, c_vp]),
     "mdg_static_scratch_bytes": (c_size, []),
     "mdg_batch_workspace_size": (c_size, [_P_PROB, c_int]),

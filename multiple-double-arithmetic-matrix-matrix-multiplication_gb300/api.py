@@ -352,3 +352,58 @@ def generate(dist, p, rows, cols, seed, e0=0, e1=0, scale_rows=False, scale_cols
     check(lib().mdg_generate(d, p, rows, cols, int(seed) & (2 ** 64 - 1), e0, e1, _ptr(out), ld,
                              _stream(stream)), "mdg_generate")
     return out
+
+
+class Plan:
+    """One problem shape with its own workspace and schedule (mdg_plan_*).
+    tune(A, B, C) times the bit-identical schedules on these operands and
+    records the fastest in the library's tuning cache; later plans of the
+    same shape class start from it."""
+
+    def __init__(self, form, p, m, n, k, **kw):
+        self.form, self.p, self.m, self.n, self.k = FORMS[form], p, m, n, k
+        h = ctypes.c_void_p()
+        check(lib().mdg_plan_create(self.form, p, m, n, k, ctypes.byref(_opts(**kw)),
+                                    ctypes.byref(h)), "mdg_plan_create")
+        self.h = h
+
+    def _args(self, A, B, C):
+        return (_ptr(A), max(self.k, 1), _ptr(B), max(self.n, 1), _ptr(C), max(self.n, 1))
+
+    def tune(self, A, B, C, stream=None):
+        check(lib().mdg_plan_tune(self.h, *self._args(A, B, C), _stream(stream)), "mdg_plan_tune")
+        return C
+
+    def run(self, A, B, C=None, stream=None):
+        if C is None:
+            C = torch.empty((self.m, self.n, self.p), dtype=torch.float64, device=A.device)
+        check(lib().mdg_plan_run(self.h, *self._args(A, B, C), _stream(stream)), "mdg_plan_run")
+        return C
+
+    def schedule(self):
+        o = Options()
+        check(lib().mdg_plan_schedule(self.h, ctypes.byref(o)), "mdg_plan_schedule")
+        return {"engine": o.engine, "parts": o.parts, "raster": o.raster}
+
+    def close(self):
+        if self.h:
+            lib().mdg_plan_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
+def tune_cache_save(path):
+    check(lib().mdg_tune_cache_save(str(path).encode()), "mdg_tune_cache_save")
+
+
+def tune_cache_load(path):
+    check(lib().mdg_tune_cache_load(str(path).encode()), "mdg_tune_cache_load")
+
+
+def tune_cache_clear():
+    lib().mdg_tune_cache_clear()
+
+
+def tune_cache_size():
+    return lib().mdg_tune_cache_size()

@@ -40,6 +40,12 @@ int engine_choice(int opt) {
   return 1;
 }
 
+bool alloc_over_limit(size_t bytes) {
+  const char *e = std::getenv("MDG_ALLOC_LIMIT_BYTES");
+  if (!e || !*e) return false;
+  return bytes > std::strtoull(e, nullptr, 10);
+}
+
 // ------------------------------------------------------------------ cache --
 // Grow-only device buffers owned by the library, for calls that take no
 // workspace argument (mdg_gemm_host, mdg_scale_exponents).  One per slot.
@@ -87,6 +93,7 @@ struct DeviceCache {
   }
   int get(int slot, size_t bytes, void **out) {
     if (bytes == 0) bytes = 256;
+    if (alloc_over_limit(bytes)) return MDG_ERROR_ALLOCATION;
     if (cap[slot] < bytes) {
       if (ptr[slot]) cudaFree(ptr[slot]);
       ptr[slot] = nullptr;
@@ -342,10 +349,13 @@ int mdg_gemm_host(int form, int p, int m, int n, int k, const double *A, const d
   Opts o;
   MDG_TRY(resolve_opts(p, opt, &o));
   if (m == 0 || n == 0) return MDG_SUCCESS;
-  std::lock_guard<std::mutex> lk(g_cache.mu);
-  MDG_TRY(g_cache.bind_device());
   const size_t sa = sizeof(double) * (size_t)m * k * p, sb = sizeof(double) * (size_t)k * n * p,
                sc = sizeof(double) * (size_t)m * n * p;
+  if (alloc_over_limit(sa) || alloc_over_limit(sb) || alloc_over_limit(sc) ||
+      alloc_over_limit(workspace_bytes(form, p, m, n, k, o)))
+    return MDG_ERROR_ALLOCATION;
+  std::lock_guard<std::mutex> lk(g_cache.mu);
+  MDG_TRY(g_cache.bind_device());
   void *dA, *dB, *dC, *ws = nullptr;
   MDG_TRY(g_cache.get(0, sa, &dA));
   MDG_TRY(g_cache.get(1, sb, &dB));

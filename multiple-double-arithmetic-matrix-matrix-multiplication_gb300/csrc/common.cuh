@@ -20,6 +20,12 @@ inline unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// Host-side fault injection: with MDG_ALLOC_LIMIT_BYTES set, every device
+// allocation the library makes for itself (the host-entry cache, plans)
+// larger than that many bytes fails with MDG_ERROR_ALLOCATION, before any
+// CUDA call (a simulated out-of-memory; nothing is asked of the device).
+bool alloc_over_limit(size_t bytes);
+
 }  // namespace mdgi
 
 #define MDG_TRY_CUDA(call)                        \

@@ -97,3 +97,19 @@ def test_schedule_options_accepted(L):
     for kw in ({"engine": "tc_pair", "parts": 8, "raster": 1000}, {"engine": "mma_sync"},
                {"engine": "tc", "parts": 1, "raster": 1}):
         assert api.workspace_size("slice_bf16", 4, 512, 512, 512, **kw) == base
+
+
+def test_allocation_cap_simulates_out_of_memory(L, monkeypatch):
+    """Host-side fault injection: MDG_ALLOC_LIMIT_BYTES makes the library's
+    own device allocations (the host entry's buffers, plan workspaces) fail
+    with MDG_ERROR_ALLOCATION before any CUDA call."""
+    import numpy as np
+    monkeypatch.setenv("MDG_ALLOC_LIMIT_BYTES", "1024")
+    A = np.zeros((64, 64, 4))
+    C = np.zeros((64, 64, 4))
+    ptr = lambda a: ctypes.c_void_p(a.ctypes.data)
+    for form in (0, 1, 2):
+        assert L.mdg_gemm_host(form, 4, 64, 64, 64, ptr(A), ptr(A), ptr(C), None) == 9
+    h = ctypes.c_void_p()
+    assert L.mdg_plan_create(2, 4, 64, 64, 64, None, ctypes.byref(h)) == 9
+    assert L.mdg_status_string(9) == b"allocation failed"
