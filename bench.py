@@ -494,6 +494,19 @@ def main():
         del a64
         forms["fp64_peak"] = {"tflops": fp64, "how": "torch.matmul float64 4096^3 (cuBLAS "
                               "DGEMM), 3 launches, CUDA events"}
+        # the INT8 tensor rate, against which an int8-digit slice form would
+        # run (cuBLAS through torch._int_mm), beside BF16 at the same size
+        a8 = torch.randint(-128, 127, (8192, 8192), dtype=torch.int8, device="cuda")
+        b8 = a8.t().contiguous().t()
+        a16 = torch.randn(8192, 8192, dtype=torch.bfloat16, device="cuda")
+        torch._int_mm(a8, b8)
+        a16 @ a16
+        t8 = event_time(lambda: torch._int_mm(a8, b8), stream, iters=3)
+        t16 = event_time(lambda: a16 @ a16, stream, iters=3)
+        forms["int8_vs_bf16"] = {"int8_tops": 2.0 * 8192 ** 3 / t8 / 1e12,
+                                 "bf16_tflops": 2.0 * 8192 ** 3 / t16 / 1e12,
+                                 "how": "torch._int_mm int8 and torch.matmul bf16, 8192^3"}
+        del a8, b8, a16
         mnk = 1024.0 ** 3
         # split form: per (row, column, k) the DMMA chunks of the 16 output
         # slices hold sum_i 4 ceil((i + 1) / 4) = 160 multiply-adds

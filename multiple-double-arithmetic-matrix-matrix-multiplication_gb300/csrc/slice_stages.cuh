@@ -263,13 +263,26 @@ __device__ __forceinline__ void renorm_elems(int s, int D, int KB, int m, int n,
         continue;
       }
       const int sh = tb > 52 ? tb - 52 : 0;
-      uint64_t mm = mdgi::wide_bits64<NW>(mag, sh) & ((1ull << 53) - 1);
-      if (sh > 0) {
-        const bool rb = (mdgi::wide_bits64<NW>(mag, sh - 1) & 1ull) != 0;
+      // one 64-bit window from bit sh - 1: the round bit, then the 53 bits
+      // of the limb (tb <= 52: the limb is word 0 itself, nothing to round)
+      const uint64_t x = sh > 0 ? mdgi::wide_bits64<NW>(mag, sh - 1) : (mag[0] << 1);
+      uint64_t mm = (x >> 1) & ((1ull << 53) - 1);
+      if (sh > 0 && (x & 1ull)) {
         const bool sticky = sh > 1 && mdgi::wide_any_below<NW>(mag, sh - 1);
-        if (rb && (sticky || (mm & 1))) mm += 1;
+        if (sticky || (mm & 1)) mm += 1;
       }
-      const double val = ldexp((double)mm, sh + scale);
+      // mm 2^(sh + scale) as a double; with the top bit at 52 (or 53 after
+      // rounding up) and a normal exponent it is assembled from its fields
+      // by integer instructions, otherwise converted and scaled in FP64
+      const bool top = mm >> 53;
+      const uint64_t frac = top ? (mm >> 1) : mm;
+      const int be = sh + scale + 52 + (top ? 1 : 0) + 1023;
+      double val;
+      if ((frac >> 52) == 1 && be >= 1 && be <= 2046)
+        val = __longlong_as_double(
+            (long long)(((uint64_t)be << 52) | (frac & ((1ull << 52) - 1))));
+      else
+        val = ldexp((double)mm, sh + scale);
       out[l] = neg ? -val : val;
       mdgi::wide_add_shifted<NW>(w[v], neg ? (int64_t)mm : -(int64_t)mm, sh);
     }
