@@ -541,7 +541,9 @@ def main():
             "config": {"workload": args.workload, "p": P, "m": m, "n": n, "k": k, "slices": s,
                        "diagonals": D, "digit_pairs": pairs, "form": "slice_bf16",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": "inputs (2 x 2 GiB) larger than L2, no flush"},
+                       "l2": f"inputs (A {A.nbytes / 2**30:.2f} GiB, B {B.nbytes / 2**30:.2f} "
+                             f"GiB, digit planes {2 * s * m * k * 2 / 1e9:.1f} GB) larger "
+                             "than L2 (129 MB), no flush"},
             "e2e": {"value": flops * world / t_e2e / 1e9, "unit": UNIT,
                     "h2d_bytes_per_step": A.nbytes + B.nbytes,
                     "d2h_bytes_per_step": m * n * P * 8,
@@ -553,8 +555,8 @@ def main():
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_sust,
                          "unit": "TFLOP/s", "frac": achieved / bf16_sust,
                          "traffic": DIAG_TRAFFIC_BYTES.get(args.workload),
-                         "traffic_note": "DRAM bytes per launch, one-pass ncu capture; the "
-                                         "operands are 2 x 3.76 GB of digit planes",
+                         "traffic_note": "DRAM bytes per launch, one-pass ncu capture of this "
+                                         "workload (null where none was taken)",
                          "kernel": "diag_gemm", "kernel_ms": t_diag * 1e3,
                          "algorithmic_tflop_per_launch": tflop,
                          "peak_kind": f"{peak_kind} bf16 sustained"},
