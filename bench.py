@@ -431,6 +431,9 @@ def main():
 
     # ---- host link bandwidth and a pipelined host-to-host loop (copies of
     # step i+1 and of the result of step i overlap the GEMM of step i)
+    # the first copy after a pause runs far below the link's warm rate on
+    # these hosts; report both
+    t_h2d_first = event_time(lambda: dA.copy_(hA, non_blocking=True), stream, iters=1)
     t_h2d = event_time(lambda: dA.copy_(hA, non_blocking=True), stream, iters=2)
     pipe = pipelined_e2e(api, hA, hB, hC, P, m, n, k, need, steps=max(2, min(args.steps, 3)))
 
@@ -550,6 +553,7 @@ def main():
                     "call": "mdg_gemm_host (pinned host buffers; B, then A in row panels "
                             "overlapped with the GEMM, C panels copied back behind it)",
                     "h2d_gbs": A.nbytes / t_h2d / 1e9,
+                    "h2d_gbs_first_copy": A.nbytes / t_h2d_first / 1e9,
                     "pipelined_value": flops * world / pipe / 1e9,
                     "pipelined": "mdg_gemm on two device buffer sets; H2D of step i+1 and D2H of step i on copy streams overlap the GEMM of step i"},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_sust,
