@@ -359,7 +359,7 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
       for (int d = 0; d < jb.D; ++d) {
         const int S = mdgi::diag_pairs(d, jb.s) * jb.KB;
         for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
-          // lane 0 waits; the verdict is broadcast so the warp stays
+          // lane 0 waits; the outcome is broadcast so the warp stays
           // converged for the .sync.aligned TMEM loads
           int ok = 1;
           if (lane == 0) ok = mbar_wait(accfull(buf), aph[buf], abort_flag) ? 1 : 0;
@@ -447,7 +447,10 @@ __global__ void __launch_bounds__(THREADS, 1)
 // arrive, multicast, on the empty and accumulator-full barriers of both
 // CTAs; the epilogue warps of both CTAs arrive on the even CTA's
 // accumulator-empty barrier (16 arrivals).  Each CTA's TMEM holds its 128
-// rows of both accumulators.
+// rows of both accumulators.  Warps: 0 producer, 1 MMA issuer (even CTA),
+// 2-9 epilogue, 10 the pacer (even CTA; see "Pacing across clusters").
+// Work units are tiles, or parts of tiles (ranges of diagonals), taken in
+// strips of `raster` column blocks.
 constexpr int TN2 = 256, BH = 128;
 constexpr int STAGES2 = 6;
 constexpr int A2_BYTES = TM * TK * 2;  // 16 KiB
