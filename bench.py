@@ -166,6 +166,25 @@ def cpu_sample(P, A, B, target_s, threads):
     return 2.0 * r * nc * k / dt / 1e9, f"{r} rows x {nc} columns of C at k={k}", dt
 
 
+def cpu_cudant_sample(P, A, B, n=256):
+    """The reference's CPU convolution path (TCcudant.cpp: split4pd, splitp,
+    manualconvmult) through the oracle's restatement of its loops, on the
+    leading n x n x n block, one thread like the reference: effective
+    md-GFLOP/s of the split-form product it forms (its 4P slice planes are
+    not squeezed back to P limbs)."""
+    import oracle
+    pp = 4 * P
+    As = oracle.split("split4", P, A[:n, :n].reshape(-1, P)).reshape(n, n, pp)
+    Bs = oracle.split("split4", P, B[:n, :n].reshape(-1, P)).reshape(n, n, pp)
+    Ap = np.ascontiguousarray(np.moveaxis(As, 2, 0))
+    Bp = np.ascontiguousarray(np.moveaxis(Bs, 2, 0))
+    t0 = time.perf_counter()
+    oracle.plane_conv(n, pp, Ap, Bp)
+    dt = time.perf_counter() - t0
+    return {"value": 2.0 * n ** 3 / dt / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n}^3 block, {pp} slice planes, manualconvmult order", "seconds": dt}
+
+
 def run_reference(args):
     """The reference's CPU path, timed on the host cores."""
     world, rank = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
@@ -533,7 +552,8 @@ def main():
     if not args.no_cpu and rank == 0:
         v, sample, _ = cpu_sample(P, A, B, 6.0, os.cpu_count() or 1)
         cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": sample}
+               "sample": sample,
+               "cudant_conv": cpu_cudant_sample(P, A, B) if P <= 4 else None}
 
     if rank == 0:
         line = {
