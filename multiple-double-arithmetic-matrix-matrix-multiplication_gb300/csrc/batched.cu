@@ -28,8 +28,17 @@
 
 #include "batched_table.cuh"
 
+// Problems of one limb count P: a contiguous range of the problem table
+// (sorted by P), digit and renorm kernels launched with its own integer width.
+struct BatchGroup {
+  int p = 0, nw = 4;
+  int digA0 = 0, digA = 0, digB0 = 0, digB = 0, out0 = 0, out = 0;  // first block, blocks
+  int max_Kp = 0, max_n = 0;
+};
+
 struct mdg_batch_s {
   int count = 0, nw = 4, total_tiles = 0;
+  std::vector<BatchGroup> groups;
   int total_rowblk = 0, total_colblk = 0, total_digA = 0, total_digB = 0, total_out = 0;
   int max_k = 0, max_n = 0, max_Kp = 0;
   int total_exps = 0;
@@ -95,7 +104,15 @@ int plan_batch(const mdg_problem *problems, int count, Layout *L, mdg_batch_s *h
   L->off_chunks.resize(count);
   int rowblk = 0, colblk = 0, digA = 0, digB = 0, outr = 0, tiles = 0, offE = 0, offF = rows;
   h->nw = 4;
-  for (int i = 0; i < count; ++i) {
+  h->groups.clear();
+  // the table is built in order of P (stable), so that every P group is one
+  // contiguous range of blocks for the digit and renorm launches
+  std::vector<int> order(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return problems[a].p < problems[b].p; });
+  for (int oi = 0; oi < count; ++oi) {
+    const int i = order[oi];
     const mdg_problem &q = problems[i];
     const int s = mdg_default_slices(q.p), D = s;
     const int Mp = (int)mdgi::align_up(std::max(q.m, 1), 128);
@@ -108,6 +125,21 @@ int plan_batch(const mdg_problem *problems, int count, Layout *L, mdg_batch_s *h
     const int nw = std::max(mdgi::words_for(s, 1), mdgi::words_for(1, D));
     if (!nw) return MDG_ERROR_NOT_SUPPORTED;
     h->nw = std::max(h->nw, nw);
+    if (h->groups.empty() || h->groups.back().p != q.p) {
+      BatchGroup g;
+      g.p = q.p;
+      g.digA0 = digA;
+      g.digB0 = digB;
+      g.out0 = outr;
+      h->groups.push_back(g);
+    }
+    BatchGroup &grp = h->groups.back();
+    grp.nw = std::max(grp.nw, nw);
+    grp.digA += Mp;
+    grp.digB += Np;
+    grp.out += std::max(q.m, 1);
+    grp.max_Kp = std::max(grp.max_Kp, Kp);
+    grp.max_n = std::max(grp.max_n, q.n);
     if (ws) {
       BatchProblem b{};
       b.p = q.p; b.s = s; b.D = D; b.m = q.m; b.n = q.n; b.k = q.k;
@@ -253,20 +285,35 @@ int mdg_batch_run(mdg_batch_s *h, void *stream) {
   MDG_TRY_LAUNCH();
   exps_b<<<mdgi::ceil_div(h->total_exps, 256), 256, 0, st>>>(h->total_exps, h->bits, h->exps);
   MDG_TRY_LAUNCH();
-  const dim3 ga(h->total_digA, mdgi::ceil_div(h->max_Kp, 128));
-  const dim3 gb(h->total_digB, mdgi::ceil_div(h->max_Kp, 128));
-  const dim3 gr(h->total_out, mdgi::ceil_div(h->max_n, 128));
-#define MDG_BATCH_NW(W)                                                            \
-  MDG_TRY(mdgi::launch_batch_digits<W>(h->dprobs, h->count, h->exps, ga, gb, st));  \
-  MDG_TRY(mdgi::launch_diag_gemm_grouped(h->dgroups, h->count, h->total_tiles, st)); \
-  MDG_TRY(mdgi::launch_batch_renorm<W>(h->dprobs, h->count, h->exps, gr, st));
-  switch (h->nw) {
-    case 4: MDG_BATCH_NW(4); break;
-    case 6: MDG_BATCH_NW(6); break;
-    case 10: MDG_BATCH_NW(10); break;
-    default: MDG_BATCH_NW(16); break;
+  // digits and renorm per P group, each with its own integer width
+  for (const BatchGroup &g : h->groups) {
+    if (!g.digA && !g.digB) continue;
+    const dim3 ga(std::max(g.digA, 1), mdgi::ceil_div(g.max_Kp, 128));
+    const dim3 gb(std::max(g.digB, 1), mdgi::ceil_div(g.max_Kp, 128));
+#define MDG_BATCH_DIGITS(W) \
+  MDG_TRY(mdgi::launch_batch_digits<W>(h->dprobs, h->count, h->exps, ga, gb, g.digA0, g.digB0, st))
+    switch (g.nw) {
+      case 4: MDG_BATCH_DIGITS(4); break;
+      case 6: MDG_BATCH_DIGITS(6); break;
+      case 10: MDG_BATCH_DIGITS(10); break;
+      default: MDG_BATCH_DIGITS(16); break;
+    }
+#undef MDG_BATCH_DIGITS
   }
-#undef MDG_BATCH_NW
+  MDG_TRY(mdgi::launch_diag_gemm_grouped(h->dgroups, h->count, h->total_tiles, st));
+  for (const BatchGroup &g : h->groups) {
+    if (!g.out || !g.max_n) continue;
+#define MDG_BATCH_RENORM(W)                                                                   \
+  MDG_TRY(mdgi::launch_batch_renorm<W>(g.p, h->dprobs, h->count, h->exps, g.out, g.max_n, g.out0, \
+                                       st))
+    switch (g.nw) {
+      case 4: MDG_BATCH_RENORM(4); break;
+      case 6: MDG_BATCH_RENORM(6); break;
+      case 10: MDG_BATCH_RENORM(10); break;
+      default: MDG_BATCH_RENORM(16); break;
+    }
+#undef MDG_BATCH_RENORM
+  }
   return MDG_SUCCESS;
 }
 

@@ -42,13 +42,14 @@ __device__ __forceinline__ int find_problem(const BatchProblem *pr, int count, i
   return lo;
 }
 
-// Digits of every A and B, and the renormalisation of every C, with NW-word
+// Digits of the A and B of one P group (digit-row blocks from xa / xb),
+// and the renormalisation of its C (`rows` output rows from x0), with NW-word
 // integers (instantiated in batched_w{4,6,10,16}.cu).
 template <int NW>
 int launch_batch_digits(const BatchProblem *pr, int count, const int *E, dim3 ga, dim3 gb,
-                        cudaStream_t st);
+                        int xa, int xb, cudaStream_t st);
 template <int NW>
-int launch_batch_renorm(const BatchProblem *pr, int count, const int *E, dim3 gr,
-                        cudaStream_t st);
+int launch_batch_renorm(int p, const BatchProblem *pr, int count, const int *E, int rows,
+                        int max_n, int x0, cudaStream_t st);
 
 }  // namespace mdgi

@@ -3,6 +3,6 @@
 #include "batched_stages.cuh"
 
 template int mdgi::launch_batch_digits<4>(const mdgi::BatchProblem *, int, const int *, dim3,
-                                           dim3, cudaStream_t);
-template int mdgi::launch_batch_renorm<4>(const mdgi::BatchProblem *, int, const int *, dim3,
-                                           cudaStream_t);
+                                           dim3, int, int, cudaStream_t);
+template int mdgi::launch_batch_renorm<4>(int, const mdgi::BatchProblem *, int, const int *,
+                                           int, int, int, cudaStream_t);
