@@ -201,6 +201,7 @@ static int run_split_gemm(int p, const Opts &o, int m, int n, int k, const doubl
   double *Aq = reinterpret_cast<double *>(base + sp.off_Aq);
   double *Bq = reinterpret_cast<double *>(base + sp.off_Bq);
   double *Cq = reinterpret_cast<double *>(base + sp.off_Cq);
+  NvtxRange range("mdg fp64split");
   MDG_TRY(launch_split(o.split_kind, o.split_exact, p, (long long)m * k, Ac, Aq, 0, 0, st));
   MDG_TRY(launch_split(o.split_kind, o.split_exact, p, (long long)k * n, Bc, Bq, 0, 0, st));
   MDG_TRY(launch_slice_conv(sp.pp, m, n, k, Aq, Bq, Cq, 0, st));
@@ -232,6 +233,7 @@ using namespace mdgi;
 // stream and the blocking streams, as the single-stream path would.
 static int host_slice_panels(int p, const Opts &o, int m, int n, int k, const double *A,
                              const double *B, double *C, double *dA, double *dB, double *dC) {
+  NvtxRange range("mdg host: B, then A panels overlapped");
   const int want = std::min(kMaxPanels, m / 1024);
   const int mp = (int)align_up((m + want - 1) / want, 256);
   const int panels = (m + mp - 1) / mp;
@@ -330,8 +332,10 @@ int mdg_gemm(int form, int p, int m, int n, int k, const double *A, int lda, con
     MDG_TRY_CUDA(cudaMemset2DAsync(C, sizeof(double) * ldc * p, 0, sizeof(double) * n * p, m, st));
     return MDG_SUCCESS;
   }
-  if (form == MDG_FORM_PLAIN)
+  if (form == MDG_FORM_PLAIN) {
+    NvtxRange range("mdg plain");
     return launch_plain_gemm(p, m, n, k, A, lda, B, ldb, C, ldc, st);
+  }
   const size_t need = workspace_bytes(form, p, m, n, k, o);
   if (!workspace || workspace_bytes_ < need) return MDG_ERROR_WORKSPACE;
   if (form == MDG_FORM_FP64_SPLIT)

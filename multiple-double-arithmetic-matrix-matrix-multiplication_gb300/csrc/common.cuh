@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include "mdg_arith.h"
@@ -17,6 +18,16 @@ inline bool valid_p(int p) { return p == 2 || p == 4 || p == 8 || p == 16; }
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 inline unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+
+// An NVTX range for the scope (host side): names the stages of a GEMM in
+// profiler timelines and lets ncu select them (--nvtx --nvtx-include).
+// Without a tool attached the calls return at once.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 

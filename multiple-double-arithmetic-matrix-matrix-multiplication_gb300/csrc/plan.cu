@@ -185,6 +185,7 @@ int mdg_plan_tune(mdg_plan plan, const double *A, int lda, const double *B, int 
     MDG_TRY_CUDA(cudaStreamSynchronize(mdgi::as_stream(stream)));
     return MDG_SUCCESS;
   }
+  mdgi::NvtxRange range("mdg plan tune");
   // schedules with the same bits: CTA pairs (engine 2) with parts auto / 1 /
   // 2 / 4, and single CTAs (engine 1)
   const int cand[5][2] = {{2, 0}, {2, 1}, {2, 2}, {2, 4}, {1, 0}};

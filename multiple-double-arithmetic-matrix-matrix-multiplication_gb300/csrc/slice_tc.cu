@@ -395,12 +395,17 @@ int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *
   void *dA = base + pl.off_dA;
   void *dB = base + pl.off_dB;
   auto *Cd = reinterpret_cast<int *>(base + pl.off_Cd);
-  MDG_TRY(launch_scale_exponents(pl.p, pl.m, pl.n, pl.k, A, lda, B, ldb, rowbits, colbits, E, F,
-                                 st));
-  MDG_TRY(launch_digits(pl.p, pl.s, pl.m, pl.k, A, lda, E, 0, dA, pl.Kp, pl.plane_a, pl.Mp,
-                        pl.Kp, st));
-  MDG_TRY(launch_digits(pl.p, pl.s, pl.n, pl.k, B, ldb, F, 1, dB, pl.Kp, pl.plane_b, pl.Np,
-                        pl.Kp, st));
+  NvtxRange range("mdg slice_bf16");
+  {
+    NvtxRange r("split: scale exponents and digits");
+    MDG_TRY(launch_scale_exponents(pl.p, pl.m, pl.n, pl.k, A, lda, B, ldb, rowbits, colbits, E,
+                                   F, st));
+    MDG_TRY(launch_digits(pl.p, pl.s, pl.m, pl.k, A, lda, E, 0, dA, pl.Kp, pl.plane_a, pl.Mp,
+                          pl.Kp, st));
+    MDG_TRY(launch_digits(pl.p, pl.s, pl.n, pl.k, B, ldb, F, 1, dB, pl.Kp, pl.plane_b, pl.Np,
+                          pl.Kp, st));
+  }
+  NvtxRange r2("diagonal GEMM and renormalisation");
   if (engine != 0) {
     MDG_TRY(launch_diag_gemm_tc(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
                                 pl.plane_b, Cd, pl.plane_c, engine == 2 ? 1 : 0, parts, raster, st));
