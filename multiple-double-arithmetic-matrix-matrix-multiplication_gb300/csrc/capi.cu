@@ -231,8 +231,24 @@ using namespace mdgi;
 // behind the tensor-core work.  Bits as one mdg_gemm (slice_panel).  The
 // work starts after everything queued before it on the legacy default
 // stream and the blocking streams, as the single-stream path would.
+static int host_slice_panels_issue(int p, const Opts &o, int m, int n, int k, const double *A,
+                                   const double *B, double *C, double *dA, double *dB,
+                                   double *dC);
+
 static int host_slice_panels(int p, const Opts &o, int m, int n, int k, const double *A,
                              const double *B, double *C, double *dA, double *dB, double *dC) {
+  const int st = host_slice_panels_issue(p, o, m, n, k, A, B, C, dA, dB, dC);
+  if (st != MDG_SUCCESS)
+    // copies into the caller's host buffers may still be queued: let them
+    // finish before returning, so that the caller may free the buffers
+    for (cudaStream_t s : g_cache.streams)
+      if (s) cudaStreamSynchronize(s);
+  return st;
+}
+
+static int host_slice_panels_issue(int p, const Opts &o, int m, int n, int k, const double *A,
+                                   const double *B, double *C, double *dA, double *dB,
+                                   double *dC) {
   NvtxRange range("mdg host: B, then A panels overlapped");
   const int want = std::min(kMaxPanels, m / 1024);
   const int mp = (int)align_up((m + want - 1) / want, 256);
