@@ -220,6 +220,8 @@ def ref():
         R.ref_squeeze.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_long, _dp, _dp]
         R.ref_mat.argtypes = [ctypes.c_uint, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]
         R.ref_bigB2.argtypes = [_dp, ctypes.c_int, ctypes.c_int, _dp]
+        R.ref_host.argtypes = [ctypes.c_int] * 4 + [_dp, _dp, _dp]
+        R.ref_host.restype = ctypes.c_long
         _ref = R
     return _ref
 
@@ -277,6 +279,21 @@ def ref_bigB2(Bq, n, pp):
     out = np.zeros((n * pp) * (n * pp), dtype=np.float64)
     ref().ref_bigB2(_ptr(Bq), n, pp, _ptr(out))
     return out
+
+
+REF_HOST = {"part": 0, "bigA": 1, "bigB": 2, "matmulhost": 3, "renormhost": 4,
+            "renormhostbig": 5}
+
+
+def ref_host(name, n, p, A, B=None, i=0):
+    """The reference's layout helper / host function `name` (TCcuda.h:33-81)
+    on n P-doubles (part) or n x n P-doubles (the others)."""
+    A = _f64(A)
+    B = _f64(B) if B is not None else np.zeros(1)
+    out = np.zeros(max(A.size, (n * p) ** 2), dtype=np.float64)
+    got = ref().ref_host(REF_HOST[name], n, p, i, _ptr(A), _ptr(B), _ptr(out))
+    assert got >= 0, name
+    return out[:got].copy()
 
 
 def ref_cudant_conv(how, n, pp, A, B):

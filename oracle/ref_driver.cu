@@ -153,4 +153,29 @@ int ref_bigB2(const double *Bq, int n, int pp, double *out) {
   return 0;
 }
 
+/* Layout helpers and host functions of TCcuda.cu (TCcuda.h:33-81):
+ * which 0 part(x, p, i) of n P-doubles, 1 bigA(A, n, p), 2 bigB(B, n, p),
+ * 3 matmulhost(A, B, n, p), 4 renormhost(A, n, p), 5 renormhostbig(A, n, p)
+ * (the last two in place on a copy).  Returns the number of doubles
+ * written to out, -1 for an unknown `which`. */
+long ref_host(int which, int n, int p, int i, const double *A, const double *B, double *out) {
+  const size_t np2 = (size_t)n * n * p;
+  vector<double> a(A, A + (which == 0 ? (size_t)n * p : np2)), o;
+  switch (which) {
+    case 0: o = part(a, p, i); break;
+    case 1: o = bigA(a, n, p); break;
+    case 2: o = bigB(a, n, p); break;
+    case 3: {
+      vector<double> b(B, B + np2);
+      o = matmulhost(a, b, n, p);
+      break;
+    }
+    case 4: renormhost(a, n, p); o = a; break;
+    case 5: renormhostbig(a, n, p); o = a; break;
+    default: return -1;
+  }
+  memcpy(out, o.data(), sizeof(double) * o.size());
+  return (long)o.size();
+}
+
 }  // extern "C"

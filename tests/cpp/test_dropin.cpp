@@ -42,6 +42,18 @@ int main(int argc, char **argv) {
     save(argv[5], bigB2(load(argv[4]), atoi(argv[2]), atoi(argv[3])));
   } else if (cmd == "squeeze") {  // squeeze <p> <pp> <in> <out>
     save(argv[5], pllntsqueeze(load(argv[4]), atoi(argv[2]), atoi(argv[3])));
+  } else if (cmd == "host") {  // host <name> <p> <n> <A> <B> <out>: TCcuda.h:33-81
+    const std::string name = argv[2];
+    const int p = atoi(argv[3]), n = atoi(argv[4]);
+    vector<double> A = load(argv[5]), B = load(argv[6]), out;
+    if (name == "part1") out = part(A, p, 1);
+    else if (name == "bigA") out = bigA(A, n, p);
+    else if (name == "bigB") out = bigB(B, n, p);
+    else if (name == "matmulhost") out = matmulhost(A, B, n, p);
+    else if (name == "renormhost") { renormhost(A, n, p); out = A; }
+    else if (name == "renormhostbig") { renormhostbig(A, n, p); out = A; }
+    else return 3;
+    save(argv[7], out);
   } else if (cmd == "bits") {  // bits <x> : bitform / double_rep round trip
     const double x = atof(argv[2]);
     printf("%.17g\n", double_rep(bitform(x)));

@@ -5,7 +5,8 @@ from its sources by oracle/Makefile into oracle/_ref (the sources must be
 present, so this script runs in the build container only).  Inputs come
 from the seeded generators of the library's inputs module.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py              # every file
+    python tests/golden/make_golden.py hostfuncs    # hostfuncs_P*.npz only
 
 Files (numpy .npz):
   arith_P{2,4,8,16}.npz   add/mul/sub/div/sqrt/inc_d/mul_d of 256 pairs
@@ -17,6 +18,8 @@ Files (numpy .npz):
   mat_seed.npz            srand(seed); mat(n, p) (TCcuda.cu:14)
   bigB2.npz               bigB2 block-Toeplitz matrix (TCcuda.cu:79-95)
   cudant.npz              TCcudant.cpp split4pd + manualconvmult/directdotconv
+  hostfuncs_P{2,4}.npz    part, bigA, bigB, matmulhost, renormhost, renormhostbig
+                          (TCcuda.cu host functions, TCcuda.h:33-81)
 """
 import importlib
 import os
@@ -106,5 +109,27 @@ def main():
                         direct=oracle.ref_cudant_conv(1, n, 4 * P, Ap, Bp))
 
 
+def hostfuncs():
+    """The reference's layout helpers and host-side functions on small
+    signed inputs (own seed, so the other files stay as they are)."""
+    oracle.build(ref=True)
+    rng = np.random.default_rng(20241203)
+    for P, n in ((2, 5), (4, 4)):
+        A = mixed(rng, n * n, P).reshape(n, n, P)
+        B = mixed(rng, n * n, P).reshape(n, n, P)
+        d = {"A": A, "B": B, "n": n, "P": P,
+             "part1": oracle.ref_host("part", n * n, P, A, i=1),
+             "bigA": oracle.ref_host("bigA", n, P, A),
+             "bigB": oracle.ref_host("bigB", n, P, B),
+             "matmulhost": oracle.ref_host("matmulhost", n, P, A, B),
+             "renormhost": oracle.ref_host("renormhost", n, P, A),
+             "renormhostbig": oracle.ref_host("renormhostbig", n, P, A)}
+        np.savez_compressed(os.path.join(HERE, f"hostfuncs_P{P}.npz"), **d)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["hostfuncs"]:
+        hostfuncs()
+    else:
+        main()
+        hostfuncs()

@@ -67,6 +67,22 @@ def test_host_squeeze_matches_reference(prog, tmp_path, P, pp):
     assert np.array_equal(np.fromfile(tmp_path / "y.bin").reshape(g["y"].shape), g["y"])
 
 
+@pytest.mark.parametrize("P", [2, 4])
+@pytest.mark.parametrize("name", ["part1", "bigA", "bigB", "matmulhost", "renormhost",
+                                  "renormhostbig"])
+def test_host_layout_and_renorm_functions_match_reference(prog, tmp_path, P, name):
+    """part, bigA, bigB, matmulhost, renormhost and renormhostbig of the
+    drop-in against the reference's own functions (TCcuda.h:33-81)."""
+    g = np.load(os.path.join(GOLDEN, f"hostfuncs_P{P}.npz"))
+    g["A"].tofile(tmp_path / "A.bin")
+    g["B"].tofile(tmp_path / "B.bin")
+    run(prog, "host", name, P, int(g["n"]), tmp_path / "A.bin", tmp_path / "B.bin",
+        tmp_path / "o.bin")
+    got = np.fromfile(tmp_path / "o.bin")
+    assert np.array_equal(got, g[name])
+    assert np.array_equal(np.signbit(got), np.signbit(g[name]))
+
+
 REF_DRIVER = "/root/reference/C++/TCtest.cu"
 
 
