@@ -27,9 +27,10 @@ static void save(const char *path, const vector<double> &v) {
 int main(int argc, char **argv) {
   if (argc < 2) return 2;
   const std::string cmd = argv[1];
-  if (cmd == "mat") {  // mat <n> <p> <seed> <out>
+  if (cmd == "mat") {  // mat <n> <p> <seed> <out> [<expmin> <expmax>]
     srand((unsigned)atoi(argv[4]));
-    save(argv[5], mat(atoi(argv[2]), atoi(argv[3])));
+    const int e0 = argc > 7 ? atoi(argv[6]) : 0, e1 = argc > 7 ? atoi(argv[7]) : 0;
+    save(argv[5], mat(atoi(argv[2]), atoi(argv[3]), e0, e1));
   } else if (cmd == "matmul") {  // matmul <p> <n> <A> <B> <out>
     const int p = atoi(argv[2]), n = atoi(argv[3]);
     vector<double> A = load(argv[4]), B = load(argv[5]), C;

@@ -20,6 +20,7 @@ Files (numpy .npz):
   cudant.npz              TCcudant.cpp split4pd + manualconvmult/directdotconv
   hostfuncs_P{2,4}.npz    part, bigA, bigB, matmulhost, renormhost, renormhostbig
                           (TCcuda.cu host functions, TCcuda.h:33-81)
+  mat_seed_range.npz      srand(seed); mat(n, p, expmin, expmax) with expmin < expmax
 """
 import importlib
 import os
@@ -125,6 +126,9 @@ def hostfuncs():
              "renormhost": oracle.ref_host("renormhost", n, P, A),
              "renormhostbig": oracle.ref_host("renormhostbig", n, P, A)}
         np.savez_compressed(os.path.join(HERE, f"hostfuncs_P{P}.npz"), **d)
+    # mat / random_pd with an exponent range: rand() % (expmax - expmin) drawn per entry
+    np.savez_compressed(os.path.join(HERE, "mat_seed_range.npz"), seed=11, n=4, P=4,
+                        expmin=-6, expmax=5, out=oracle.ref_mat(11, 4, 4, -6, 5))
 
 
 if __name__ == "__main__":

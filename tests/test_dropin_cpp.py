@@ -41,6 +41,17 @@ def test_mat_reproduces_reference_rand_sequence(prog, tmp_path):
     assert np.array_equal(np.fromfile(out).reshape(g["out"].shape), g["out"])
 
 
+def test_mat_with_exponent_range_reproduces_reference(prog, tmp_path):
+    g = np.load(os.path.join(GOLDEN, "mat_seed_range.npz"))
+    out = tmp_path / "mat.bin"
+    run(prog, "mat", int(g["n"]), int(g["P"]), int(g["seed"]), out, int(g["expmin"]),
+        int(g["expmax"]))
+    got = np.fromfile(out).reshape(g["out"].shape)
+    assert np.array_equal(got, g["out"])
+    e = np.frexp(got[..., 0])[1]
+    assert e.min() >= int(g["expmin"]) and e.max() < int(g["expmax"])
+
+
 @pytest.mark.parametrize("P", [2, 4, 8, 16])
 def test_host_matmul_matches_reference(prog, tmp_path, P):
     g = np.load(os.path.join(GOLDEN, f"matmul_P{P}.npz"))
