@@ -21,6 +21,7 @@ Files (numpy .npz):
   hostfuncs_P{2,4}.npz    part, bigA, bigB, matmulhost, renormhost, renormhostbig
                           (TCcuda.cu host functions, TCcuda.h:33-81)
   mat_seed_range.npz      srand(seed); mat(n, p, expmin, expmax) with expmin < expmax
+  squeeze_P2_pp12.npz     dd squeeze of the 12 partials of mixsplit2
 """
 import importlib
 import os
@@ -126,6 +127,10 @@ def hostfuncs():
              "renormhost": oracle.ref_host("renormhost", n, P, A),
              "renormhostbig": oracle.ref_host("renormhostbig", n, P, A)}
         np.savez_compressed(os.path.join(HERE, f"hostfuncs_P{P}.npz"), **d)
+    # the double-double squeeze of the mixed split (12 partials per entry)
+    parts = oracle.ref_split("mix", 2, mixed(rng, 48, 2)) * 3.0
+    np.savez_compressed(os.path.join(HERE, "squeeze_P2_pp12.npz"), x=parts,
+                        y=oracle.ref_squeeze(2, 12, parts))
     # mat / random_pd with an exponent range: rand() % (expmax - expmin) drawn per entry
     np.savez_compressed(os.path.join(HERE, "mat_seed_range.npz"), seed=11, n=4, P=4,
                         expmin=-6, expmax=5, out=oracle.ref_mat(11, 4, 4, -6, 5))

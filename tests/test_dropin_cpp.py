@@ -70,7 +70,7 @@ def test_bigB2_matches_reference(prog, tmp_path):
     assert np.array_equal(np.fromfile(tmp_path / "o.bin"), g["out"])
 
 
-@pytest.mark.parametrize("P,pp", [(2, 8), (4, 32), (8, 64), (16, 128)])
+@pytest.mark.parametrize("P,pp", [(2, 8), (2, 12), (4, 32), (8, 64), (16, 128)])
 def test_host_squeeze_matches_reference(prog, tmp_path, P, pp):
     g = np.load(os.path.join(GOLDEN, f"squeeze_P{P}_pp{pp}.npz"))
     g["x"].tofile(tmp_path / "x.bin")

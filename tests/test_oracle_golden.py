@@ -63,7 +63,7 @@ def test_mixsplit_matches_reference(orc):
     assert np.array_equal(np.signbit(out), np.signbit(g["out"]))
 
 
-@pytest.mark.parametrize("P,pp", [(2, 8), (2, 16), (4, 16), (4, 32), (8, 32), (8, 64),
+@pytest.mark.parametrize("P,pp", [(2, 8), (2, 12), (2, 16), (4, 16), (4, 32), (8, 32), (8, 64),
                                   (16, 64), (16, 128)])
 def test_squeeze_matches_reference(orc, P, pp):
     g = load(f"squeeze_P{P}_pp{pp}.npz")
