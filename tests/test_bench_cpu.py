@@ -1,0 +1,16 @@
+"""The CPU legs of bench.py on tiny inputs (no GPU): the plain-GEMM sample
+of the oracle port, the TCcudant convolution sample, and the peaks file."""
+import importlib
+
+import numpy as np
+
+
+def test_cpu_baseline_legs_run_on_small_inputs(inputs, orc):
+    bench = importlib.import_module("bench")
+    P, A, B = inputs.workload("qd1024", 64, 64, 128)
+    value, sample, dt = bench.cpu_sample(P, A, B, 0.05, 2)
+    assert value > 0 and dt > 0 and "rows" in sample
+    conv = bench.cpu_cudant_sample(P, A, B, n=32)
+    assert conv["value"] > 0 and conv["cores"] == 1 and conv["kind"] == "port"
+    peaks = bench.peaks()
+    assert len(peaks) == 4 and all(isinstance(v, float) for v in peaks[:3])
