@@ -113,3 +113,37 @@ def test_allocation_cap_simulates_out_of_memory(L, monkeypatch):
     h = ctypes.c_void_p()
     assert L.mdg_plan_create(2, 4, 64, 64, 64, None, ctypes.byref(h)) == 9
     assert L.mdg_status_string(9) == b"allocation failed"
+
+
+def test_plain_c_program_builds_and_links(tmp_path):
+    """The C ABI from C99: the header compiles with -pedantic, and a C
+    program linked against libmdgemm.so calls entries that need no GPU."""
+    import os
+    import shutil
+    import subprocess
+    from conftest import ROOT
+    cc = shutil.which("gcc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    lib = pkg("_lib").LIB_PATH
+    src = tmp_path / "abi.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <string.h>\n#include "mdgemm.h"\n'
+        "int main(void) {\n"
+        "  mdg_options o;\n  memset(&o, 0, sizeof o);\n"
+        "  if (mdg_version() < 100) return 1;\n"
+        "  if (mdg_default_slices(4) != 28) return 2;\n"
+        "  if (mdg_gemm(MDG_FORM_PLAIN, 3, 4, 4, 4, NULL, 4, NULL, 4, NULL, 4, &o, NULL, 0, NULL)\n"
+        "      != MDG_ERROR_INVALID_LIMBS) return 3;\n"
+        '  printf("%s\\n", mdg_status_string(MDG_ERROR_WORKSPACE));\n'
+        "  return 0;\n}\n")
+    exe = tmp_path / "abi"
+    libdir = os.path.dirname(lib)
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                    "-I", os.path.join(ROOT, "include"), "-I", "/usr/local/cuda/include",
+                    str(src), "-L", libdir, "-lmdgemm", "-Wl,-rpath," + libdir, "-o", str(exe)],
+                   check=True, capture_output=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    assert "workspace" in r.stdout
