@@ -6,7 +6,8 @@ present, so this script runs in the build container only).  Inputs come
 from the seeded generators of the library's inputs module.
 
     python tests/golden/make_golden.py              # every file
-    python tests/golden/make_golden.py hostfuncs    # hostfuncs_P*.npz only
+    python tests/golden/make_golden.py hostfuncs    # hostfuncs_P{2,4}, squeeze_P2_pp12, mat_seed_range
+    python tests/golden/make_golden.py hostfuncs_wide   # hostfuncs_P{8,16}.npz only
 
 Files (numpy .npz):
   arith_P{2,4,8,16}.npz   add/mul/sub/div/sqrt/inc_d/mul_d of 256 pairs
@@ -18,7 +19,7 @@ Files (numpy .npz):
   mat_seed.npz            srand(seed); mat(n, p) (TCcuda.cu:14)
   bigB2.npz               bigB2 block-Toeplitz matrix (TCcuda.cu:79-95)
   cudant.npz              TCcudant.cpp split4pd + manualconvmult/directdotconv
-  hostfuncs_P{2,4}.npz    part, bigA, bigB, matmulhost, renormhost, renormhostbig
+  hostfuncs_P{2,4,8,16}.npz  part, bigA, bigB, matmulhost, renormhost, renormhostbig
                           (TCcuda.cu host functions, TCcuda.h:33-81)
   mat_seed_range.npz      srand(seed); mat(n, p, expmin, expmax) with expmin < expmax
   squeeze_P2_pp12.npz     dd squeeze of the 12 partials of mixsplit2
@@ -136,9 +137,31 @@ def hostfuncs():
                         expmin=-6, expmax=5, out=oracle.ref_mat(11, 4, 4, -6, 5))
 
 
+def hostfuncs_wide():
+    """The same host functions at P = 8 and 16 (own seed, so the files of
+    ``hostfuncs`` stay as they are)."""
+    oracle.build(ref=True)
+    rng = np.random.default_rng(20241204)
+    for P in (8, 16):
+        n = 4
+        A = mixed(rng, n * n, P).reshape(n, n, P)
+        B = mixed(rng, n * n, P).reshape(n, n, P)
+        d = {"A": A, "B": B, "n": n, "P": P,
+             "part1": oracle.ref_host("part", n * n, P, A, i=1),
+             "bigA": oracle.ref_host("bigA", n, P, A),
+             "bigB": oracle.ref_host("bigB", n, P, B),
+             "matmulhost": oracle.ref_host("matmulhost", n, P, A, B),
+             "renormhost": oracle.ref_host("renormhost", n, P, A),
+             "renormhostbig": oracle.ref_host("renormhostbig", n, P, A)}
+        np.savez_compressed(os.path.join(HERE, f"hostfuncs_P{P}.npz"), **d)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["hostfuncs"]:
         hostfuncs()
+    elif sys.argv[1:] == ["hostfuncs_wide"]:
+        hostfuncs_wide()
     else:
         main()
         hostfuncs()
+        hostfuncs_wide()

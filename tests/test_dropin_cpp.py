@@ -78,7 +78,7 @@ def test_host_squeeze_matches_reference(prog, tmp_path, P, pp):
     assert np.array_equal(np.fromfile(tmp_path / "y.bin").reshape(g["y"].shape), g["y"])
 
 
-@pytest.mark.parametrize("P", [2, 4])
+@pytest.mark.parametrize("P", [2, 4, 8, 16])
 @pytest.mark.parametrize("name", ["part1", "bigA", "bigB", "matmulhost", "renormhost",
                                   "renormhostbig"])
 def test_host_layout_and_renorm_functions_match_reference(prog, tmp_path, P, name):
