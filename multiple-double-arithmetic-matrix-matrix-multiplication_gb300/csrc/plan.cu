@@ -100,6 +100,13 @@ struct Json {
   }
 };
 
+// v is a whole number in [lo, hi] (NaN and infinities are not)
+bool whole_in(double v, int lo, int hi, int *out) {
+  if (!(v >= lo && v <= hi) || v != (double)(int)v) return false;
+  *out = (int)v;
+  return true;
+}
+
 std::string quoted(const std::string &s) {
   std::string q = "\"";
   for (char c : s) {
@@ -261,13 +268,18 @@ int mdg_tune_cache_load(const char *path) {
   const bool ok = js.object([&](const std::string &dev) {
     return js.object([&](const std::string &shape) {
       TuneEntry e;
+      // schedule fields are whole numbers in the ranges mdg_gemm accepts, so
+      // a loaded entry can never make a later plan of that shape fail
       const bool fields = js.object([&](const std::string &field) {
         double v;
         if (!js.num(&v)) return false;
-        if (field == "engine") e.engine = (int)v;
-        else if (field == "parts") e.parts = (int)v;
-        else if (field == "raster") e.raster = (int)v;
-        else if (field == "ms") e.ms = v;
+        if (field == "engine") return whole_in(v, 0, 3, &e.engine);
+        if (field == "parts") return whole_in(v, 0, 8, &e.parts);
+        if (field == "raster") return whole_in(v, 0, 1 << 20, &e.raster);
+        if (field == "ms") {
+          if (!(v >= 0.0 && v <= 1e12)) return false;
+          e.ms = v;
+        }
         return true;
       });
       if (fields) parsed[dev][shape] = e;

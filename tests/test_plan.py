@@ -39,6 +39,14 @@ def test_tune_cache_rejects_bad_files(tmp_path):
     for text in ("{", "[]", '{"a": {"b": {"engine": "x"}}}', '{"a": 1}', '{"a": {}} trailing'):
         bad.write_text(text)
         assert L.mdg_tune_cache_load(str(bad).encode()) == 4, text
+    # schedule values outside what mdg_gemm accepts reject the whole file
+    for field, value in (("engine", "1e300"), ("engine", "-1"), ("engine", "4"),
+                         ("engine", "nan"), ("parts", "9"), ("parts", "1.5"),
+                         ("raster", "-1"), ("raster", "inf"), ("raster", "2e6"),
+                         ("ms", "-1"), ("ms", "nan")):
+        bad.write_text('{"d": {"ok": {"engine": 2, "parts": 1}, '
+                       f'"s": {{"{field}": {value}}}}}}}')
+        assert L.mdg_tune_cache_load(str(bad).encode()) == 4, (field, value)
     assert L.mdg_tune_cache_load(str(tmp_path / "missing.json").encode()) == 7
     assert L.mdg_tune_cache_load(None) == 3
     assert L.mdg_tune_cache_size() == 0
