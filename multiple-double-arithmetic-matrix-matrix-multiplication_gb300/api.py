@@ -33,6 +33,35 @@ def _opts(slices=0, diagonals=0, split_kind="split4", split_exact=True, engine="
     return o
 
 
+def _need(cond, msg, exc=ValueError):
+    if not cond:
+        raise exc(msg)
+
+
+def _device_pd(X, name, shape=None, device=None):
+    """X must be a float64 CUDA tensor (rows, cols, P), of `shape` and on
+    `device` where those are given: the library reads and writes exactly
+    that many entries, so a mismatch is an error here, not a stray access."""
+    _need(isinstance(X, torch.Tensor) and X.is_cuda, f"{name} must be a CUDA tensor", TypeError)
+    _need(X.dtype == torch.float64, f"{name} must be float64, not {X.dtype}", TypeError)
+    _need(X.dim() == 3, f"{name} must be (rows, cols, P), not {tuple(X.shape)}")
+    if shape is not None:
+        _need(tuple(X.shape) == tuple(shape),
+              f"{name} is {tuple(X.shape)}, expected {tuple(shape)}")
+    if device is not None:
+        _need(X.device == device, f"{name} is on {X.device}, expected {device}")
+
+
+def _pair(A, B, what):
+    """(m, n, k, p) of the product A (m, k, P) B (k, n, P) of device tensors."""
+    _device_pd(A, f"{what}: A")
+    _device_pd(B, f"{what}: B", device=A.device)
+    m, k, p = A.shape
+    _need(B.shape[0] == k and B.shape[2] == p,
+          f"{what}: A {tuple(A.shape)} and B {tuple(B.shape)} do not chain")
+    return m, B.shape[1], k, p
+
+
 def _stream(stream):
     s = stream if stream is not None else torch.cuda.current_stream()
     return ctypes.c_void_p(s.cuda_stream)
@@ -57,12 +86,13 @@ def workspace_size(form, p, m, n, k, **kw):
 
 
 def gemm(A, B, form="slice_bf16", out=None, workspace=None, stream=None, **kw):
-    """C = A @ B for device tensors A (m, k, P) and B (k, n, P)."""
-    assert A.is_cuda and B.is_cuda and A.dtype == torch.float64 and B.dtype == torch.float64
-    m, k, p = A.shape
-    k2, n, p2 = B.shape
-    assert k == k2 and p == p2
+    """C = A @ B for device tensors A (m, k, P) and B (k, n, P); `out`, when
+    given, is a contiguous (m, n, P) tensor on the same device."""
+    m, n, k, p = _pair(A, B, "gemm")
     A, B = A.contiguous(), B.contiguous()
+    if out is not None:
+        _device_pd(out, "gemm: out", (m, n, p), A.device)
+        _need(out.is_contiguous(), "gemm: out must be contiguous")
     C = out if out is not None else torch.empty((m, n, p), dtype=torch.float64, device=A.device)
     opt = _opts(**kw)
     need = lib().mdg_gemm_workspace_size(FORMS[form], p, m, n, k, ctypes.byref(opt))
@@ -77,7 +107,9 @@ def gemm(A, B, form="slice_bf16", out=None, workspace=None, stream=None, **kw):
 def _ld(X, p):
     """Leading dimension (entries) of a (rows, cols, p) view whose rows may be
     padded: the entries of a row and the limbs of an entry must be dense."""
-    assert X.stride(2) == 1 and (X.shape[1] <= 1 or X.stride(1) == p)
+    _need(X.stride(2) == 1 and (X.shape[1] <= 1 or X.stride(1) == p)
+          and (X.shape[0] <= 1 or (X.stride(0) % p == 0 and X.stride(0) >= X.shape[1] * p)),
+          f"rows of a {tuple(X.shape)} view with strides {X.stride()} are not dense")
     return max(X.stride(0) // p if X.shape[0] > 1 else X.shape[1], X.shape[1], 1)
 
 
@@ -87,13 +119,18 @@ def gemm_ex(A, B, form="slice_bf16", trans_a=False, trans_b=False, C=None, accum
     addition), through mdg_gemm_ex.  A is (m, k, P), or (k, m, P) with
     trans_a; B is (k, n, P), or (n, k, P) with trans_b; views with padded
     rows pass their row stride as the leading dimension."""
+    _device_pd(A, "gemm_ex: A")
+    _device_pd(B, "gemm_ex: B", device=A.device)
     p = A.shape[2]
     m, k = (A.shape[1], A.shape[0]) if trans_a else (A.shape[0], A.shape[1])
     n = B.shape[0] if trans_b else B.shape[1]
-    assert (B.shape[1] if trans_b else B.shape[0]) == k and B.shape[2] == p
+    _need((B.shape[1] if trans_b else B.shape[0]) == k and B.shape[2] == p,
+          f"gemm_ex: op(A) of {tuple(A.shape)} and op(B) of {tuple(B.shape)} do not chain")
     if C is None:
-        assert not accumulate
+        _need(not accumulate, "gemm_ex: accumulate needs C")
         C = torch.empty((m, n, p), dtype=torch.float64, device=A.device)
+    else:
+        _device_pd(C, "gemm_ex: C", (m, n, p), A.device)
     opt = _opts(**kw)
     f = FORMS[form]
     need = lib().mdg_gemm_ex_workspace_size(f, int(trans_a), int(trans_b), int(accumulate), p, m,
@@ -112,7 +149,10 @@ def gemm_host(A, B, form="slice_bf16", **kw):
     out inside the call)."""
     A = np.ascontiguousarray(A, dtype=np.float64)
     B = np.ascontiguousarray(B, dtype=np.float64)
+    _need(A.ndim == 3 and B.ndim == 3, "gemm_host: A and B must be (rows, cols, P) arrays")
     m, k, p = A.shape
+    _need(B.shape[0] == k and B.shape[2] == p,
+          f"gemm_host: A {A.shape} and B {B.shape} do not chain")
     n = B.shape[1]
     C = np.empty((m, n, p), dtype=np.float64)
     check(lib().mdg_gemm_host(FORMS[form], p, m, n, k, A.ctypes.data, B.ctypes.data,
@@ -124,8 +164,7 @@ def gemm_batched(problems, form="plain", stream=None, **kw):
     """problems: list of (A, B) device tensor pairs; returns the list of C."""
     Cs, table, keep = [], (Problem * len(problems))(), []
     for i, (A, B) in enumerate(problems):
-        m, k, p = A.shape
-        n = B.shape[1]
+        m, n, k, p = _pair(A, B, f"gemm_batched: problem {i}")
         A, B = A.contiguous(), B.contiguous()
         C = torch.empty((m, n, p), dtype=torch.float64, device=A.device)
         keep += [A, B]
@@ -150,8 +189,7 @@ class BatchPlan:
         self.Cs, self.keep = [], []
         table = (Problem * len(problems))()
         for i, (A, B) in enumerate(problems):
-            m, k, p = A.shape
-            n = B.shape[1]
+            m, n, k, p = _pair(A, B, f"BatchPlan: problem {i}")
             A, B = A.contiguous(), B.contiguous()
             C = torch.empty((m, n, p), dtype=torch.float64, device=A.device)
             self.keep += [A, B]
@@ -194,8 +232,16 @@ def matmulTCnt(A, B, n, nfrag, p, loop_ct=1):
     return C.cpu().numpy().reshape(-1), e0.elapsed_time(e1)
 
 
+def _entries(x, width, what):
+    """x (host array or tensor) as a dense float64 CUDA tensor of whole
+    entries of `width` doubles each."""
+    x = _dev(x) if isinstance(x, torch.Tensor) else _dev(np.asarray(x, dtype=np.float64))
+    _need(x.numel() % width == 0, f"{what}: {x.numel()} doubles are not whole entries of {width}")
+    return x
+
+
 def _split(kind, x, p, exact=False):
-    x = _dev(np.asarray(x, dtype=np.float64).reshape(-1, p)) if not isinstance(x, torch.Tensor) else x.contiguous()
+    x = _entries(x, p, "split")
     count = x.numel() // p
     pp = {0: 4 * p, 1: 8 * p, 2: 12, 3: 4 * p}[kind]
     out = torch.empty((count, pp), dtype=torch.float64, device=x.device)
@@ -228,7 +274,7 @@ def split_planes(kind, x, p, exact=False):
     """Slices as planes: (pp, count) with plane j holding slice j of every
     entry; kind as in mdg_split (3 = splitp(split4pd(x), 4p) of
     TCcudant.cpp:163-183)."""
-    x = _dev(np.asarray(x, dtype=np.float64).reshape(-1, p)) if not isinstance(x, torch.Tensor) else x.contiguous()
+    x = _entries(x, p, "split_planes")
     count = x.numel() // p
     pp = {0: 4 * p, 1: 8 * p, 2: 12, 3: 4 * p}[kind]
     out = torch.empty((pp, count), dtype=torch.float64, device=x.device)
@@ -241,7 +287,11 @@ def plane_conv(A, B):
     """C_i = sum_{j<=i} A_j B_{i-j} on slice planes (FP64 tensor cores); A
     (pp, m, k), B (pp, k, n) device tensors -> C (pp, m, n): manualconvmult /
     directdotconv of TCcudant.cpp:216-276."""
+    _device_pd(A, "plane_conv: A")
+    _device_pd(B, "plane_conv: B", device=A.device)
     pp, m, k = A.shape
+    _need(B.shape[0] == pp and B.shape[1] == k,
+          f"plane_conv: A {tuple(A.shape)} and B {tuple(B.shape)} do not chain")
     n = B.shape[2]
     C = torch.empty((pp, m, n), dtype=torch.float64, device=A.device)
     check(lib().mdg_plane_conv(pp, m, n, k, _ptr(A.contiguous()), _ptr(B.contiguous()), _ptr(C),
@@ -251,7 +301,7 @@ def plane_conv(A, B):
 
 def pllsqueeze_old(x, p, pp):
     """Squeeze of pp partial sums per entry into p-doubles (TCcuda.cu:908)."""
-    x = _dev(np.asarray(x, dtype=np.float64).reshape(-1)) if not isinstance(x, torch.Tensor) else x.contiguous()
+    x = _entries(x, pp, "pllsqueeze_old")
     count = x.numel() // pp
     y = torch.empty((count, p), dtype=torch.float64, device=x.device)
     check(lib().mdg_squeeze(p, pp, count, _ptr(x), _ptr(y), _stream(None)), "mdg_squeeze")
@@ -261,8 +311,7 @@ def pllsqueeze_old(x, p, pp):
 def slice_conv(Aq, Bq):
     """Truncated slice convolution on FP64 tensor cores; Aq (m, k, pp),
     Bq (k, n, pp) device tensors."""
-    m, k, pp = Aq.shape
-    n = Bq.shape[1]
+    m, n, k, pp = _pair(Aq, Bq, "slice_conv")
     Cq = torch.empty((m, n, pp), dtype=torch.float64, device=Aq.device)
     check(lib().mdg_slice_conv(pp, m, n, k, _ptr(Aq.contiguous()), _ptr(Bq.contiguous()),
                                _ptr(Cq), None, 0, _stream(None)), "mdg_slice_conv")
@@ -272,8 +321,8 @@ def slice_conv(Aq, Bq):
 # ----------------------------------------------- slice-digit stages --
 
 def scale_exponents(A, B):
-    m, k, p = A.shape
-    n = B.shape[1]
+    m, n, k, p = _pair(A, B, "scale_exponents")
+    A, B = A.contiguous(), B.contiguous()
     E = torch.empty(max(m, 1), dtype=torch.int32, device=A.device)
     F = torch.empty(max(n, 1), dtype=torch.int32, device=A.device)
     check(lib().mdg_scale_exponents(p, m, n, k, _ptr(A), max(k, 1), _ptr(B), max(n, 1), _ptr(E),
@@ -284,10 +333,15 @@ def scale_exponents(A, B):
 def slice_digits(X, E, s, trans=False):
     """BF16 digit planes: X (rows, cols, P) -> (s, rows, cols); trans=True
     takes X as (cols, rows, P) (B) and returns planes (s, n, k)."""
+    _device_pd(X, "slice_digits: X")
+    X = X.contiguous()
     if trans:
         cols, rows, p = X.shape
     else:
         rows, cols, p = X.shape
+    _need(isinstance(E, torch.Tensor) and E.is_cuda and E.dtype == torch.int32
+          and E.is_contiguous() and E.numel() >= rows,
+          f"slice_digits: E must be {rows} contiguous int32 exponents on the GPU", TypeError)
     planes = torch.empty((s, rows, cols), dtype=torch.bfloat16, device=X.device)
     check(lib().mdg_slice_digits(p, s, rows, cols, _ptr(X), X.shape[1], _ptr(E), int(trans),
                                  _ptr(planes), cols, rows * cols, _stream(None)),
@@ -299,7 +353,14 @@ def slice_diagonals(dA, dB, D):
     """Exact diagonal sums of digit planes dA (s, m, k), dB (s, n, k); m a
     multiple of 128, n of 256, k of 64.  Returns the int32 chunk planes
     (chunks, m, n) of the C ABI."""
+    for name, X in (("dA", dA), ("dB", dB)):
+        _need(isinstance(X, torch.Tensor) and X.is_cuda and X.dtype == torch.bfloat16
+              and X.dim() == 3 and X.is_contiguous(),
+              f"slice_diagonals: {name} must be contiguous (s, rows, k) bfloat16 planes",
+              TypeError)
     s, m, k = dA.shape
+    _need(dB.shape[0] == s and dB.shape[2] == k,
+          f"slice_diagonals: dA {tuple(dA.shape)} and dB {tuple(dB.shape)} do not match")
     n = dB.shape[1]
     nch = lib().mdg_slice_chunk_count(s, D, k)
     Cd = torch.empty((nch, m, n), dtype=torch.int32, device=dA.device)
@@ -323,7 +384,18 @@ def chunks_to_diagonals(Cd, s, D, k):
 
 def renorm_diagonals(Cd, E, F, p, s, D, k):
     """Round chunk planes (chunks, m, n) to P-doubles (m, n, P)."""
+    _need(isinstance(Cd, torch.Tensor) and Cd.is_cuda and Cd.dtype == torch.int32
+          and Cd.dim() == 3 and Cd.is_contiguous(),
+          "renorm_diagonals: Cd must be contiguous int32 chunk planes on the GPU", TypeError)
     _, m, n = Cd.shape
+    _need(Cd.shape[0] == lib().mdg_slice_chunk_count(s, D, k),
+          f"renorm_diagonals: {Cd.shape[0]} chunk planes, the layout of s={s} D={D} k={k} "
+          f"has {lib().mdg_slice_chunk_count(s, D, k)}")
+    for name, X, count in (("E", E, m), ("F", F, n)):
+        _need(isinstance(X, torch.Tensor) and X.is_cuda and X.dtype == torch.int32
+              and X.is_contiguous() and X.numel() >= count,
+              f"renorm_diagonals: {name} must be {count} contiguous int32 exponents on the GPU",
+              TypeError)
     C = torch.empty((m, n, p), dtype=torch.float64, device=Cd.device)
     check(lib().mdg_renorm_diagonals(p, s, D, k, m, n, _ptr(Cd), m * n, n, _ptr(E), _ptr(F),
                                      _ptr(C), n, _stream(None)), "mdg_renorm_diagonals")
@@ -348,7 +420,8 @@ def generate(dist, p, rows, cols, seed, e0=0, e1=0, scale_rows=False, scale_cols
     d = GEN_DISTS[dist] | (GEN_SCALE_ROWS if scale_rows else 0) | (GEN_SCALE_COLS if scale_cols else 0)
     if out is None:
         out = torch.empty((rows, cols, p), dtype=torch.float64, device="cuda")
-    ld = out.stride(0) // p if out.dim() == 3 and rows > 1 else max(cols, 1)
+    _device_pd(out, "generate: out", (rows, cols, p))
+    ld = _ld(out, p)
     check(lib().mdg_generate(d, p, rows, cols, int(seed) & (2 ** 64 - 1), e0, e1, _ptr(out), ld,
                              _stream(stream)), "mdg_generate")
     return out
@@ -368,16 +441,26 @@ class Plan:
         self.h = h
 
     def _args(self, A, B, C):
-        return (_ptr(A), max(self.k, 1), _ptr(B), max(self.n, 1), _ptr(C), max(self.n, 1))
+        """Operands of this plan's shape; A and B are made dense, C (written
+        in place) must be."""
+        m, n, k, p = self.m, self.n, self.k, self.p
+        _device_pd(A, "Plan: A", (m, k, p))
+        _device_pd(B, "Plan: B", (k, n, p), A.device)
+        _device_pd(C, "Plan: C", (m, n, p), A.device)
+        _need(C.is_contiguous(), "Plan: C must be contiguous")
+        A, B = A.contiguous(), B.contiguous()
+        return (A, B), (_ptr(A), max(k, 1), _ptr(B), max(n, 1), _ptr(C), max(n, 1))
 
     def tune(self, A, B, C, stream=None):
-        check(lib().mdg_plan_tune(self.h, *self._args(A, B, C), _stream(stream)), "mdg_plan_tune")
+        keep, args = self._args(A, B, C)
+        check(lib().mdg_plan_tune(self.h, *args, _stream(stream)), "mdg_plan_tune")
         return C
 
     def run(self, A, B, C=None, stream=None):
         if C is None:
             C = torch.empty((self.m, self.n, self.p), dtype=torch.float64, device=A.device)
-        check(lib().mdg_plan_run(self.h, *self._args(A, B, C), _stream(stream)), "mdg_plan_run")
+        keep, args = self._args(A, B, C)
+        check(lib().mdg_plan_run(self.h, *args, _stream(stream)), "mdg_plan_run")
         return C
 
     def schedule(self):
