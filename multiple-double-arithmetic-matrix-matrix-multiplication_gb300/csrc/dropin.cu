@@ -10,7 +10,9 @@
 // Behaviour changed: device memory is freed; any n is accepted where the
 // reference needs n % nfrag == 0 or 64 | n; the pllsqueeze / pllntsqueeze
 // dispatchers return zeros for an unsupported p (the reference has no
-// return statement on that path, TCcuda.cu:810-853).
+// return statement on that path, TCcuda.cu:810-853); a vector shorter than
+// its n x n x p (or planes) shape gives the empty / zero result instead of
+// a read past its end, on the host or, through the device copies, on the GPU.
 #include <cstdlib>
 #include <cstring>
 
@@ -30,7 +32,16 @@ struct DevBuf {
   }
 };
 
+// v holds at least `count` doubles (a negative count never fits)
+bool holds(const vector<double> &v, long long count) {
+  return count >= 0 && v.size() >= (size_t)count;
+}
+
+// n x n entries of p doubles, or -1 for a negative size
+long long nnp(int n, int p) { return (n < 0 || p < 0) ? -1 : (long long)n * n * p; }
+
 vector<double> gpu_split(int kind, vector<double> x, int p) {
+  if (p <= 0) return vector<double>();
   const int pp = kind == 0 ? 4 * p : kind == 1 ? 8 * p : 12;
   const long long count = (long long)x.size() / p;
   vector<double> out((size_t)count * pp, 0.0);
@@ -45,7 +56,9 @@ vector<double> gpu_split(int kind, vector<double> x, int p) {
 
 template <int P>
 vector<double> host_plain(const vector<double> &A, const vector<double> &B, int n) {
+  if (n < 0) return vector<double>();
   vector<double> C((size_t)n * n * P, 0.0);
+  if (!holds(A, nnp(n, P)) || !holds(B, nnp(n, P))) return C;
   for (int r = 0; r < n; ++r)
     for (int c = 0; c < n; ++c) {
       double acc[P];
@@ -59,6 +72,7 @@ vector<double> host_plain(const vector<double> &A, const vector<double> &B, int 
 
 template <int P>
 vector<double> host_squeeze(const vector<double> &x, int pp) {
+  if (pp <= 0) return vector<double>();
   const size_t n = x.size() / pp;
   vector<double> y(n * P, 0.0);
   for (size_t i = 0; i < n; ++i) {
@@ -226,6 +240,7 @@ vector<double> part(vector<double> x, int p, int i) {
 
 vector<double> bigA(vector<double> A, int n, int p) {
   vector<double> AA;
+  if (!holds(A, nnp(n, p))) return AA;
   for (int r = 0; r < n; ++r)
     for (int i = 0; i < p; ++i)
       for (int c = 0; c < n; ++c) AA.push_back(A[((size_t)r * n + c) * p + i]);
@@ -234,6 +249,7 @@ vector<double> bigA(vector<double> A, int n, int p) {
 
 vector<double> bigB(vector<double> B, int n, int p) {
   vector<double> BB;
+  if (!holds(B, nnp(n, p))) return BB;
   for (int i = 0; i < p; ++i)
     for (int c = 0; c < n; ++c)
       for (int j = 0; j < p; ++j)
@@ -244,6 +260,7 @@ vector<double> bigB(vector<double> B, int n, int p) {
 
 vector<double> bigB2(vector<double> B, int n, int p) {
   vector<double> BB;
+  if (!holds(B, nnp(n, p))) return BB;
   for (int c = 0; c < n; ++c)
     for (int i = 0; i < p; ++i)
       for (int r = 0; r < n; ++r)
@@ -276,25 +293,31 @@ __global__ void renormA(double *A, int n, int p) {
 }
 
 void renormhost(vector<double> &A, int n, int p) {
+  if (!holds(A, nnp(n, p))) return;
   for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j)
+    for (int j = 0; j < n; ++j) {
+      double *e = A.data() + ((size_t)i * n + j) * p;  // entry (i, j), limbs adjacent
       for (int k = 0; k < p - 1; ++k) {
-        const double hi = A[i * n * p + j * p + k] + A[i * n * p + j * p + k + 1];
-        const double lo = hi - A[i * n * p + j * p + k];
-        A[i * n * p + j * p + k] = hi;
-        A[i * n * p + j * p + k + 1] = lo;
+        const double hi = e[k] + e[k + 1];
+        const double lo = hi - e[k];
+        e[k] = hi;
+        e[k + 1] = lo;
       }
+    }
 }
 
 void renormhostbig(vector<double> &A, int n, int p) {
+  if (!holds(A, nnp(n, p))) return;
   for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j)
+    for (int j = 0; j < n; ++j) {
+      double *e = A.data() + (size_t)i * n * p + j;  // row i, column j: limbs n apart
       for (int k = 0; k < p - 1; ++k) {
-        const double hi = A[i * n * p + k * n + j] + A[i * n * p + (k + 1) * n + j];
-        const double lo = hi - A[i * n * p + k * n + j];
-        A[i * n * p + k * n + j] = hi;
-        A[i * n * p + (k + 1) * n + j] = lo;
+        const double hi = e[(size_t)k * n] + e[(size_t)(k + 1) * n];
+        const double lo = hi - e[(size_t)k * n];
+        e[(size_t)k * n] = hi;
+        e[(size_t)(k + 1) * n] = lo;
       }
+    }
 }
 
 // One thread per entry C(r, c) with r from x and c from y, as the
@@ -322,6 +345,7 @@ vector<double> matmulTCnt(vector<double> A, vector<double> B, int n, int nfrag, 
   t_CUDA = 0.0f;
   if (!mdgi::valid_p(p) || n <= 0) return C;
   const size_t sz = (size_t)n * n * p;
+  if (!holds(A, nnp(n, p)) || !holds(B, nnp(n, p))) return C;
   DevBuf dA(sz), dB(sz), dC(sz);
   if (!dA.p || !dB.p || !dC.p) return C;
   cudaMemcpy(dA.p, A.data(), sz * sizeof(double), cudaMemcpyHostToDevice);
@@ -348,6 +372,7 @@ vector<double> matmulTC(vector<double> A, vector<double> B, int n, int p, int fo
   t_CUDA = 0.0f;
   if (!mdgi::valid_p(p) || n <= 0) return C;
   const size_t sz = (size_t)n * n * p;
+  if (!holds(A, nnp(n, p)) || !holds(B, nnp(n, p))) return C;
   DevBuf dA(sz), dB(sz), dC(sz);
   const size_t ws_bytes = mdg_gemm_workspace_size(form, p, n, n, n, opt);
   void *ws = nullptr;
@@ -374,7 +399,9 @@ vector<double> matmulTC(vector<double> A, vector<double> B, int n, int p, int fo
 // Naive FP64 slice convolution without error-free transformations
 // (TCcuda.cu:304-318).
 vector<double> matmulhost(vector<double> A, vector<double> B, int n, int p) {
+  if (nnp(n, p) < 0) return vector<double>();
   vector<double> C = zeros(n, n, p);
+  if (!holds(A, nnp(n, p)) || !holds(B, nnp(n, p))) return C;
   for (int r = 0; r < n; ++r)
     for (int c = 0; c < n; ++c)
       for (int k = 0; k < n; ++k)
@@ -460,8 +487,10 @@ namespace {
 // device cannot be used.
 vector<double> gpu_plane_conv(const vector<double> &A, const vector<double> &B, int pp, int m,
                               int n, int k) {
+  if (pp <= 0 || m < 0 || n < 0 || k < 0) return vector<double>();
   vector<double> C((size_t)pp * m * n, 0.0);
-  if (pp <= 0 || m <= 0 || n <= 0) return C;
+  if (m == 0 || n == 0) return C;
+  if (!holds(A, (long long)pp * m * k) || !holds(B, (long long)pp * k * n)) return C;
   DevBuf dA(A.size()), dB(B.size()), dC(C.size());
   if ((A.size() && !dA.p) || (B.size() && !dB.p) || !dC.p) return C;
   cudaMemcpy(dA.p, A.data(), A.size() * sizeof(double), cudaMemcpyHostToDevice);
@@ -503,6 +532,9 @@ void matmul2(vector<double> A, vector<double> B, vector<double> &C, int n) {
 }
 
 void convmult2(vector<double> A, vector<double> B, vector<double> &C_aux, int n, int p) {
+  if (n < 0 || p <= 0 || !holds(A, nnp(n, p)) || !holds(B, nnp(n, p)) ||
+      !holds(C_aux, nnp(n, p) * p))
+    return;
   const size_t nn = (size_t)n * n;
   for (int i = 0; i < p; ++i)
     for (int j = 0; j < p; ++j) {
@@ -515,6 +547,7 @@ void convmult2(vector<double> A, vector<double> B, vector<double> &C_aux, int n,
 }
 
 void convadd2(vector<double> &C, vector<double> &C_aux, int n, int p) {
+  if (n < 0 || p <= 0 || !holds(C, nnp(n, p)) || !holds(C_aux, nnp(n, p) * p)) return;
   const size_t nn = (size_t)n * n;
   for (int i = 0; i < p; ++i)
     for (size_t e = 0; e < nn; ++e)

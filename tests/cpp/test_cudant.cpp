@@ -9,6 +9,7 @@
 //   twostep.bin convmult2 + convadd2 into zeros
 //   accum.bin   dotconvbutbetter into a matrix of ones
 //   matmul.bin  matmul2 of the first planes into a matrix of ones
+#include <cstdio>
 #include <cstdlib>
 #include <fstream>
 #include <string>
@@ -30,6 +31,25 @@ static void save(const std::string &path, const vector<double> &v) {
 }
 
 int main(int argc, char **argv) {
+  if (argc == 2 && std::string(argv[1]) == "short") {
+    // operands one plane entry short: the two-step path leaves C and C_aux as
+    // they are, the one-step paths return zeros without touching the device
+    const int n = 3, p = 2;
+    const vector<double> S((size_t)n * n * p - 1, 1.0), F((size_t)n * n * p, 1.0);
+    vector<double> aux = zeros(n, p * p), C = zeros(n, p);
+    convmult2(S, F, aux, n, p);
+    vector<double> aux_short((size_t)n * n * p * p - 1, 0.0);
+    convmult2(F, F, aux_short, n, p);
+    convadd2(C, aux_short, n, p);
+    double t = 0.0;
+    for (double x : aux) t += x;
+    for (double x : aux_short) t += x;
+    for (double x : C) t += x;
+    for (double x : manualconvmult(S, F, n, p)) t += x;
+    for (double x : directdotconv(F, S, n, p)) t += x;
+    printf("short %g\n", t);
+    return 0;
+  }
   if (argc != 6) return 2;
   const int p = atoi(argv[1]), n = atoi(argv[2]), pp = 4 * p;
   const std::string out = argv[5];

@@ -55,6 +55,28 @@ int main(int argc, char **argv) {
     else if (name == "renormhostbig") { renormhostbig(A, n, p); out = A; }
     else return 3;
     save(argv[7], out);
+  } else if (cmd == "short") {  // short <p> <n>: n x n x p operands one double short
+    const int p = atoi(argv[2]), n = atoi(argv[3]);
+    const vector<double> S((size_t)n * n * p - 1, 1.0), F((size_t)n * n * p, 1.0);
+    auto sum = [](const vector<double> &v) {
+      double t = 0.0;
+      for (double x : v) t += x;
+      return t;
+    };
+    vector<double> R = S, Rb = S;
+    renormhost(R, n, p);
+    renormhostbig(Rb, n, p);
+    float t = 1.0f;
+    const vector<double> C1 = matmulhost(S, F, n, p), C2 = matmulhost(F, S, n, p);
+    const vector<double> C3 = matmulTCnt(S, F, n, 8, p, 1, t);
+    printf("bigA %zu\nbigB %zu\nbigB2 %zu\n", bigA(S, n, p).size(), bigB(S, n, p).size(),
+           bigB2(S, n, p).size());
+    printf("matmulhost %zu %g %zu %g\n", C1.size(), sum(C1), C2.size(), sum(C2));
+    printf("renormhost %g\nrenormhostbig %g\n", sum(R), sum(Rb));
+    printf("matmulTCnt %zu %g %g\n", C3.size(), sum(C3), (double)t);
+    if (p == 2) printf("matmulddf %g\n", sum(matmulddf(S, F, n)));
+    if (p == 4) printf("matmulqdf %g\n", sum(matmulqdf(F, S, n)));
+    printf("pllntsqueeze %zu\n", pllntsqueeze(F, p, 0).size());
   } else if (cmd == "bits") {  // bits <x> : bitform / double_rep round trip
     const double x = atof(argv[2]);
     printf("%.17g\n", double_rep(bitform(x)));

@@ -34,6 +34,14 @@ def test_driver_builds_with_host_compiler(prog):
     assert os.path.exists(prog)
 
 
+def test_short_operands_leave_outputs_alone(prog):
+    """Plane operands one entry shorter than n x n x p: nothing is read or
+    written past their end; convmult2 / convadd2 leave their outputs as they
+    are and the one-step products return zeros before any device copy."""
+    r = subprocess.run([prog, "short"], check=True, capture_output=True, text=True, timeout=60)
+    assert r.stdout.strip() == "short 0"
+
+
 def bound(Ap, Bp):
     """Per-entry bound on the difference of two FP64 summation orders of the
     truncated convolution: 2^-50 * sum_{j<=i} |A_j| |B_{i-j}|."""

@@ -94,6 +94,25 @@ def test_host_layout_and_renorm_functions_match_reference(prog, tmp_path, P, nam
     assert np.array_equal(np.signbit(got), np.signbit(g[name]))
 
 
+@pytest.mark.parametrize("P", [2, 4])
+def test_short_operands_give_empty_or_zero_results(prog, P):
+    """Vectors one double shorter than their n x n x p shape (the reference
+    reads past their end): the layout builders return empty vectors, the
+    products zeros, the in-place renormalisations leave the vector as it is,
+    and the GPU product returns before any device copy."""
+    n = 3
+    full = n * n * P
+    r = subprocess.run([prog, "short", str(P), str(n)], check=True, capture_output=True,
+                       text=True, timeout=60)
+    got = dict(line.split(" ", 1) for line in r.stdout.strip().splitlines())
+    assert got["bigA"] == got["bigB"] == got["bigB2"] == "0"
+    assert got["matmulhost"] == f"{full} 0 {full} 0"
+    assert float(got["renormhost"]) == float(got["renormhostbig"]) == full - 1  # all ones kept
+    assert got["matmulTCnt"] == f"{full} 0 0"
+    assert got["matmulddf" if P == 2 else "matmulqdf"] == "0"
+    assert got["pllntsqueeze"] == "0"
+
+
 REF_DRIVER = "/root/reference/C++/TCtest.cu"
 
 
