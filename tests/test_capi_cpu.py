@@ -147,3 +147,43 @@ def test_plain_c_program_builds_and_links(tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stderr
     assert "workspace" in r.stdout
+
+
+def _table(probs):
+    Problem = pkg("_lib").Problem
+    t = (Problem * len(probs))()
+    for i, (p, m, n, k) in enumerate(probs):
+        # stand-in pointers: every call below returns before touching them
+        t[i] = Problem(p, m, n, k, 16, 16, 16, max(k, 1), max(n, 1), max(n, 1))
+    return t
+
+
+def test_batch_plan_sizes_and_arguments(L):
+    """The batched plan (mdg_batch_*) and the one-call batched entry size
+    their workspace and check every problem on the host; mixed P including
+    hexa-double is accepted."""
+    t = _table([(16, 40, 50, 70), (2, 32, 32, 32), (8, 100, 300, 64), (4, 1, 1, 1)])
+    full = L.mdg_batch_workspace_size(t, 4)
+    assert full > 0
+    sizes = [L.mdg_batch_workspace_size(t, c) for c in range(1, 5)]
+    assert sizes == sorted(set(sizes)) and sizes[-1] == full  # each problem adds its planes
+    assert L.mdg_gemm_batched_workspace_size(2, t, 4, None) == full
+    assert L.mdg_batch_workspace_size(t, 0) == 0
+    assert L.mdg_batch_workspace_size(None, 2) == 0
+    assert L.mdg_batch_workspace_size(_table([(3, 8, 8, 8)]), 1) == 0
+    assert L.mdg_batch_workspace_size(_table([(4, 0, 8, 8)]), 1) == 0
+    h = ctypes.c_void_p()
+    assert L.mdg_batch_create(t, 4, None, 0, None, None) == 3
+    assert L.mdg_batch_create(t, 0, None, 0, None, ctypes.byref(h)) == 2
+    assert L.mdg_batch_create(_table([(3, 8, 8, 8)]), 1, None, 0, None, ctypes.byref(h)) == 1
+    assert L.mdg_batch_create(t, 4, None, full, None, ctypes.byref(h)) == 5
+    assert L.mdg_batch_create(t, 4, ctypes.c_void_p(256), full - 1, None, ctypes.byref(h)) == 5
+    assert not h.value
+    assert L.mdg_batch_run(None, None) == 3
+    L.mdg_batch_destroy(None)
+    assert L.mdg_gemm_batched(2, t, -1, None, None, 0, None) == 2
+    assert L.mdg_gemm_batched(2, t, 0, None, None, 0, None) == 0
+    assert L.mdg_gemm_batched(2, None, 3, None, None, 0, None) == 3
+    assert L.mdg_gemm_batched(2, _table([(3, 8, 8, 8)]), 1, None, None, 0, None) == 1
+    assert L.mdg_gemm_batched(7, t, 4, None, None, 0, None) == 4
+    assert L.mdg_gemm_batched(2, t, 4, None, None, 0, None) == 5
