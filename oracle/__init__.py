@@ -206,7 +206,16 @@ _cudant = None
 
 
 def ref_available():
-    return os.path.exists(_REF)
+    """The reference-built libraries exist and load on this machine (a copy
+    built for another architecture does not count)."""
+    if not (os.path.exists(_REF) and os.path.exists(_CUDANT)):
+        return False
+    try:
+        ref()
+        cudant()
+    except OSError:
+        return False
+    return True
 
 
 def ref():
