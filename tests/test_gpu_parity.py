@@ -412,6 +412,20 @@ def test_batched_slice_equals_single_problem_results(api, inputs):
             assert torch.equal(C, api.gemm(A, B, "slice_bf16"))
 
 
+def test_batched_slice_hexa_double_equals_single_problem_results(api, inputs):
+    """Hexa-double problems (16-word digit and renorm kernels) in one batch
+    with other limb counts, including a 1 x 3 x 5 problem."""
+    rng = np.random.default_rng(5)
+    probs = [(16, 40, 50, 70), (16, 130, 260, 64), (8, 33, 17, 100), (2, 64, 64, 64),
+             (16, 1, 3, 5)]
+    ops = [(dev(inputs.uniform_pd(rng, (m, k), P)), dev(inputs.uniform_pd(rng, (k, n), P)))
+           for P, m, n, k in probs]
+    Cs = api.gemm_batched(ops, "slice_bf16")
+    for (A, B), C in zip(ops, Cs):
+        assert torch.equal(C, api.gemm(A, B, "slice_bf16"))
+    assert api.device_status() == 0
+
+
 def test_batched_plan_graph_capture(api, orc, inputs):
     """The plan's run() captured in a CUDA graph and replayed; results are
     the oracle's bits (checked on three problems)."""
