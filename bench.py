@@ -343,7 +343,10 @@ def bench_batched(api, inputs, stream):
             "md_gflop": flops / 1e9,
             "slice_graph_gflops": flops / t_graph / 1e9, "slice_graph_ms": t_graph * 1e3,
             "per_p": per_p,
-            "slice_launches_per_batch": 8,
+            # kernels per plan run: row and column maxima, exponents, then two
+            # digit kernels and one renormalisation per limb count, and the
+            # grouped diagonal GEMM (plus one memset of the maxima)
+            "slice_launches_per_batch": 3 + 3 * len({pr[0] for pr in probs}) + 1,
             "plain_loop_gflops": flops / t_loop / 1e9, "plain_loop_ms": t_loop * 1e3,
             "plain_batched_gflops": flops / t_pb / 1e9, "plain_batched_ms": t_pb * 1e3,
             "slice_equals_single_problem": bool(same)}
