@@ -288,6 +288,21 @@ def pipelined_e2e(api, hA, hB, hC, P, m, n, k, ws_bytes, steps):
     return dt
 
 
+def batched_tile_work(probs, slices):
+    """BF16 FLOP of the batched diagonal GEMM at the given digit counts per
+    P: useful (2 m n k per digit pair of the s diagonals kept) and as the
+    grouped kernel pads it (rows to 128, columns to 256, k to 64)."""
+    def pairs(s):
+        return sum(min(d, s - 1) - max(0, d - (s - 1)) + 1 for d in range(s))
+    up = lambda x, a: -(-x // a) * a
+    useful = padded = 0.0
+    for P, m, n, k in probs:
+        q = pairs(slices[P])
+        useful += 2.0 * m * n * k * q
+        padded += 2.0 * up(m, 128) * up(n, 256) * up(k, 64) * q
+    return useful, padded
+
+
 def bench_batched(api, inputs, stream):
     """The batched workload (256 problems, m, n, k in {32..512}, P in {2, 4, 8},
     seed 3): the BF16 slice-digit plan replayed as one CUDA graph, against a
@@ -297,6 +312,9 @@ def bench_batched(api, inputs, stream):
     ops = inputs.batched_operands(probs, rng)
     dev_ops = [(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()) for A, B in ops]
     flops = sum(2.0 * m * n * k for _, m, n, k in probs)
+    useful, padded = batched_tile_work(probs, {P: api.default_slices(P)
+                                               for P in {pr[0] for pr in probs}})
+
     def captured(pairs):
         plan = api.BatchPlan(pairs)
         plan.run()
@@ -349,7 +367,10 @@ def bench_batched(api, inputs, stream):
             "slice_launches_per_batch": 3 + 3 * len({pr[0] for pr in probs}) + 1,
             "plain_loop_gflops": flops / t_loop / 1e9, "plain_loop_ms": t_loop * 1e3,
             "plain_batched_gflops": flops / t_pb / 1e9, "plain_batched_ms": t_pb * 1e3,
-            "slice_equals_single_problem": bool(same)}
+            "slice_equals_single_problem": bool(same),
+            "diag_bf16_tflop": {"useful": useful / 1e12, "padded": padded / 1e12,
+                                "useful_frac": useful / padded,
+                                "tiles": "128 x 256 x 64 (grouped single-CTA kernel)"}}
 
 
 def main():

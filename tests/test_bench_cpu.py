@@ -14,3 +14,13 @@ def test_cpu_baseline_legs_run_on_small_inputs(inputs, orc):
     assert conv["value"] > 0 and conv["cores"] == 1 and conv["kind"] == "port"
     peaks = bench.peaks()
     assert len(peaks) == 4 and all(isinstance(v, float) for v in peaks[:3])
+
+
+def test_batched_tile_work_of_the_batched_workload(inputs):
+    """Useful and padded BF16 work of the 256-problem batch (seed 3) at the
+    default digit counts 14 / 28 / 55."""
+    bench = importlib.import_module("bench")
+    probs, _ = inputs.batched_problems(256, seed=3)
+    useful, padded = bench.batched_tile_work(probs, {2: 14, 4: 28, 8: 55})
+    assert abs(useful / 6.710e12 - 1) < 1e-3 and abs(padded / 1.168e13 - 1) < 1e-3
+    assert bench.batched_tile_work([(4, 128, 256, 64)], {4: 28}) == (2.0 * 128 * 256 * 64 * 406,) * 2
