@@ -239,8 +239,9 @@ int mdg_slice_chunk_count(int s, int D, int k);
 /* Exact diagonal sums on BF16 tensor cores: for d < D the sum over i+j=d
  * and over k of dA_i[r][k] dB_j[c][k], written as chunk planes
  * chunks[q][r][c] (int32, m x n each, chunk q of diagonal d after those of
- * diagonals 0..d-1).  dA: s planes m x ld (plane_a apart), dB: s planes
- * n x ld; m % 128 == 0, n % 256 == 0, k % 64 == 0. */
+ * diagonals 0..d-1).  dA: s planes m x ld (plane_a >= m ld apart), dB: s
+ * planes n x ld (plane_b >= n ld apart); m % 128 == 0, n % 256 == 0,
+ * k % 64 == 0. */
 int mdg_slice_diagonals(int s, int D, int m, int n, int k, const void *dA,
                         const void *dB, int ld, long long plane_a,
                         long long plane_b, int *chunks, void *stream);

@@ -581,6 +581,9 @@ int mdg_slice_diagonals(int s, int D, int m, int n, int k, const void *dA, const
                         long long plane_a, long long plane_b, int *chunks, void *stream) {
   if (s < 1 || D < 1 || D > 2 * s - 1 || m < 0 || n < 0 || k < 0) return MDG_ERROR_INVALID_SIZE;
   if (m % 128 || n % 256 || k % 64 || ld < k) return MDG_ERROR_INVALID_SIZE;
+  // each digit plane holds its rows at stride ld: planes that overlap would
+  // have the last one read past the caller's buffer
+  if (plane_a < (long long)m * ld || plane_b < (long long)n * ld) return MDG_ERROR_INVALID_SIZE;
   if (m == 0 || n == 0 || k == 0) return MDG_SUCCESS;
   if (!dA || !dB || !chunks) return MDG_ERROR_NULL_POINTER;
   const long long plane_c = (long long)m * n;

@@ -58,6 +58,11 @@ def test_bad_sizes_and_pointers_rejected(L):
     assert L.mdg_split(0, 3, 4, 4, one, one, None) == 4
     assert L.mdg_squeeze(4, 0, 4, one, one, None) == 2
     assert L.mdg_slice_diagonals(4, 4, 100, 128, 64, one, one, 64, 1, 1, one, None) == 2
+    # digit planes that would overlap (plane stride below rows x ld)
+    assert L.mdg_slice_diagonals(4, 4, 128, 256, 64, one, one, 64, 128 * 64 - 1, 256 * 64,
+                                 one, None) == 2
+    assert L.mdg_slice_diagonals(4, 4, 128, 256, 64, one, one, 64, 128 * 64, 256 * 64 - 64,
+                                 one, None) == 2
 
 
 def test_empty_problems_succeed_without_gpu(L):
