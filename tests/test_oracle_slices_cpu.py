@@ -102,16 +102,20 @@ def test_power_of_two_scaling_commutes(orc, inputs, P, j):
 
 
 @pytest.mark.parametrize("P", [2, 4, 8])
-@pytest.mark.parametrize("dist", ["uniform", "normal"])
+@pytest.mark.parametrize("dist", ["uniform", "normal", "spread"])
 def test_slice_form_not_less_accurate_than_plain(orc, inputs, P, dist):
     """Against the exact product (Python integers), the slice form at the
-    default digit count keeps at least the plain form's normwise bits."""
+    default digit count keeps at least the plain form's normwise bits, also
+    with rows of A and columns of B scaled by 2^U{-32..32} (spread)."""
     ex = pkg("errors")
     rng = np.random.default_rng(40 + P)
     m = n = k = 12
-    gen = inputs.uniform_pd if dist == "uniform" else inputs.normal_pd
+    gen = inputs.normal_pd if dist == "normal" else inputs.uniform_pd
     A = gen(rng, (m, k), P)
     B = inputs.uniform_pd(rng, (k, n), P)
+    if dist == "spread":
+        A, _ = inputs.scale_rows(rng, A)
+        B, _ = inputs.scale_cols(rng, B)
     s = SLICES[P]
     _, slice_bits = ex.error_bits(orc.gemm_slices(P, s, s, A, B, m, n, k), A, B,
                                   range(m), range(n))
