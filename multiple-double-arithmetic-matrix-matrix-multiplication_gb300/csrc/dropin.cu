@@ -476,6 +476,42 @@ __global__ void pllsqueeze_4_pp_old(double *x, double *y, int pp) { squeeze_entr
 __global__ void pllsqueeze_8_pp_old(double *x, double *y, int pp) { squeeze_entry<8>(x, y, pp); }
 __global__ void pllsqueeze_16_pp_old(double *x, double *y, int pp) { squeeze_entry<16>(x, y, pp); }
 
+// The double-double squeeze on separate partial planes (TCcuda.cu:400, 508,
+// 646): entry i of (y1, y2) takes x1[i], x2[i], ... in order through the
+// double-double inc_d.  One thread per entry and no bounds check, as in the
+// reference: the launch must cover exactly the entries.
+template <int Q>
+__device__ void squeeze_planes_dd(const double *const (&x)[Q], double *y1, double *y2) {
+  const int i = blockDim.x * blockIdx.x + threadIdx.x;
+  double acc[2] = {y1[i], y2[i]};
+#pragma unroll
+  for (int j = 0; j < Q; ++j) mdg::inc_d<2>(acc, x[j][i]);
+  y1[i] = acc[0];
+  y2[i] = acc[1];
+}
+__global__ void pllsqueeze_kernel_2_8(double *x1, double *x2, double *x3, double *x4, double *x5,
+                                      double *x6, double *x7, double *x8, double *y1,
+                                      double *y2) {
+  const double *const x[8] = {x1, x2, x3, x4, x5, x6, x7, x8};
+  squeeze_planes_dd<8>(x, y1, y2);
+}
+__global__ void pllsqueeze_kernel_2_12(double *x1, double *x2, double *x3, double *x4, double *x5,
+                                       double *x6, double *x7, double *x8, double *x9,
+                                       double *x10, double *x11, double *x12, double *y1,
+                                       double *y2) {
+  const double *const x[12] = {x1, x2, x3, x4, x5, x6, x7, x8, x9, x10, x11, x12};
+  squeeze_planes_dd<12>(x, y1, y2);
+}
+__global__ void pllsqueeze_kernel_2_16(double *x1, double *x2, double *x3, double *x4, double *x5,
+                                       double *x6, double *x7, double *x8, double *x9,
+                                       double *x10, double *x11, double *x12, double *x13,
+                                       double *x14, double *x15, double *x16, double *y1,
+                                       double *y2) {
+  const double *const x[16] = {x1, x2, x3, x4, x5, x6, x7, x8,
+                               x9, x10, x11, x12, x13, x14, x15, x16};
+  squeeze_planes_dd<16>(x, y1, y2);
+}
+
 // ------------------------------------------------------------------------
 // The CPU convolution driver's functions (include/TCcudant.h,
 // TCcudant.cpp:163-276): slicing and FP64 plane products on the GPU.

@@ -77,6 +77,17 @@ int main(int argc, char **argv) {
     if (p == 2) printf("matmulddf %g\n", sum(matmulddf(S, F, n)));
     if (p == 4) printf("matmulqdf %g\n", sum(matmulqdf(F, S, n)));
     printf("pllntsqueeze %zu\n", pllntsqueeze(F, p, 0).size());
+  } else if (cmd == "kernels") {  // kernels: every __global__ of TCcuda.h links from the library
+    const void *k[] = {(const void *)&renormbigA,           (const void *)&renormA,
+                       (const void *)&ddmm,                 (const void *)&qdmm,
+                       (const void *)&odmm,                 (const void *)&hdmm,
+                       (const void *)&pllsqueeze_kernel_2_8, (const void *)&pllsqueeze_kernel_2_12,
+                       (const void *)&pllsqueeze_kernel_2_16, (const void *)&pllsqueeze_2_pp_old,
+                       (const void *)&pllsqueeze_4_pp_old,  (const void *)&pllsqueeze_8_pp_old,
+                       (const void *)&pllsqueeze_16_pp_old};
+    int n = 0;
+    for (const void *f : k) n += f != nullptr;
+    printf("%d\n", n);
   } else if (cmd == "bits") {  // bits <x> : bitform / double_rep round trip
     const double x = atof(argv[2]);
     printf("%.17g\n", double_rep(bitform(x)));

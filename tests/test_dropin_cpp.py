@@ -113,6 +113,15 @@ def test_short_operands_give_empty_or_zero_results(prog, P):
     assert got["pllntsqueeze"] == "0"
 
 
+def test_every_declared_kernel_links(prog):
+    """The __global__ functions TCcuda.h declares (TCcuda.h:56-102) resolve
+    to libmdgemm.so: renormbigA, renormA, ddmm..hdmm, the three separate-plane
+    double-double squeezes and the four pllsqueeze_*_pp_old kernels."""
+    r = subprocess.run([prog, "kernels"], check=True, capture_output=True, text=True,
+                       timeout=60)
+    assert r.stdout.strip() == "13"
+
+
 REF_DRIVER = "/root/reference/C++/TCtest.cu"
 
 
