@@ -57,6 +57,28 @@ WORKLOADS = {
 DIAG_TRAFFIC_BYTES = {"qd8192_normal": 479.62e9, "qd4096_normal": 74.35e9}
 
 
+DEFAULT_SLICES = {2: 14, 4: 28, 8: 55, 16: 108}
+
+
+def digit_pairs(s, D):
+    """Digit pairs (i, j), i + j = d < D, of s digits per operand."""
+    return sum(min(d, s - 1) - max(0, d - (s - 1)) + 1 for d in range(D))
+
+
+def bench_config(workload, world):
+    """The `config` object of both arms' lines (the same keys and values, so
+    the two lines describe one workload)."""
+    inputs = importlib.import_module(PKG + ".inputs")
+    P, m, n, k, seed, kind = inputs.WORKLOADS[workload]
+    s = DEFAULT_SLICES[P]
+    planes_gb = s * (m + n) * k * 2 / 1e9
+    return {"workload": workload, "p": P, "m": m, "n": n, "k": k, "seed": seed,
+            "distribution": kind, "slices": s, "diagonals": s, "digit_pairs": digit_pairs(s, s),
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "l2": f"inputs (A and B {(m + n) * k * P * 8 / 2 ** 30:.2f} GiB, digit planes "
+                  f"{planes_gb:.1f} GB) larger than L2 (129 MB), no flush"}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -223,9 +245,11 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": float(np.median(times)) * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload},
+        "config": bench_config(args.workload, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                         "sample": sample},
+                         "sample": sample, "extrapolated": True,
+                         "extrapolation": "rate of the sample; the whole workload at this rate "
+                                          f"would take {2.0 * np.prod(inputs.WORKLOADS[args.workload][1:4]) / value / 1e9 / 3600:.0f} h"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -373,6 +397,143 @@ def bench_batched(api, inputs, stream):
                                 "tiles": "128 x 256 x 64 (grouped single-CTA kernel)"}}
 
 
+# FP64 operations per multi-double multiply-add of the plain form, the
+# reference's own counts (TCtest.cu:136-148: dd 23 mul + 20 add, qd 336 + 89,
+# od 1742 + 269; hd has only a placeholder there)
+PLAIN_OPS = {2: 43, 4: 425, 8: 2011}
+
+
+def split_dmma_madds(pp):
+    """(algorithmic, executed) FP64 multiply-adds per (row, column, k) of the
+    truncated slice convolution with pp slices: sum_{i<pp} (i + 1) products
+    C_i = sum_{j<=i} a_j b_{i-j}, and the 4-wide DMMA chunks the kernel runs,
+    sum_i 4 ceil((i + 1) / 4), zero lanes of partial chunks included."""
+    return pp * (pp + 1) // 2, sum(4 * -(-(i + 1) // 4) for i in range(pp))
+
+
+def bench_form_line(api, ex, stream, P, A, B, form, dA, dB, sample, iters=1, rows=None):
+    """One form on one workload: md-GFLOP/s (CUDA events, after one untimed
+    call) and error bits against the exact product on sampled entries.
+    rows: time and check only this many leading rows of C (the rate per
+    row of the plain form does not depend on the row count)."""
+    import torch
+    m, k = A.shape[:2]
+    n = B.shape[1]
+    if rows is not None and rows < m:
+        dA, A, m = dA[:rows].contiguous(), A[:rows], rows
+    out = torch.empty((m, n, P), dtype=torch.float64, device="cuda")
+    w = torch.empty(max(1, api.workspace_size(form, P, m, n, k)), dtype=torch.uint8,
+                    device="cuda")
+    api.gemm(dA, dB, form, out=out, workspace=w)
+    t = event_time(lambda: api.gemm(dA, dB, form, out=out, workspace=w), stream, iters=iters)
+    r = [i for i in sample[0] if i < m]
+    eb = ex.error_bits(out.cpu().numpy(), A, B, r, sample[1])
+    del out, w
+    torch.cuda.empty_cache()
+    return {"shape": f"{m}x{n}x{k}", "gflops": 2.0 * m * n * k / t / 1e9, "ms": t * 1e3,
+            "error_bits_entrywise": round(eb[0], 1), "error_bits_normwise": round(eb[1], 1),
+            "error_sample": f"{len(r)}x{len(sample[1])} entries, exact integer product"}
+
+
+def bench_forms(api, inputs, ex, stream):
+    """The three forms side by side on the quad-double 1024^3 (seed 1) and
+    octo-double 2048^3 row/column-spread (seed 2) workloads, the hexa-double
+    slice form against plain hd, and the FP64 and INT8 tensor rates."""
+    import torch
+    forms = {}
+    # FP64 ceiling of the two FP64 forms, measured here (the peaks file
+    # holds BF16 and HBM only): cuBLAS DGEMM through torch.matmul
+    a64 = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    torch.matmul(a64, a64)
+    t64 = event_time(lambda: torch.matmul(a64, a64), stream, iters=3)
+    fp64 = 2.0 * 4096 ** 3 / t64 / 1e12
+    del a64
+    forms["fp64_peak"] = {"tflops": fp64, "how": "torch.matmul float64 4096^3 (cuBLAS "
+                          "DGEMM), 3 launches, CUDA events"}
+    for wl in ("qd1024", "od2048_spread"):
+        P, A, B = inputs.workload(wl)
+        m, k = A.shape[:2]
+        n = B.shape[1]
+        dA, dB = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+        step = max(1, m // 6)
+        sample = (range(0, m, step), range(0, n, step))
+        block = {}
+        block["slice_bf16"] = bench_form_line(api, ex, stream, P, A, B, "slice_bf16", dA, dB,
+                                              sample, iters=3)
+        block["fp64split"] = bench_form_line(api, ex, stream, P, A, B, "fp64split", dA, dB,
+                                             sample)
+        # the plain octo-double GEMM takes ~20 s at 2048^3: rows 0..511 of C
+        block["plain"] = bench_form_line(api, ex, stream, P, A, B, "plain", dA, dB, sample,
+                                         rows=512 if P >= 8 else None)
+        if P >= 8:
+            block["plain"]["rows_timed"] = "rows 0..511 of C (full n, k)"
+        mnk = float(m) * n * k
+        alg, exe = split_dmma_madds(4 * P)
+        sp = block["fp64split"]
+        t = sp["ms"] / 1e3
+        sp["roofline"] = {"bound": "fp64 tensor (DMMA)",
+                          "achieved_tflops": 2.0 * alg * mnk / t / 1e12,
+                          "executed_tflops": 2.0 * exe * mnk / t / 1e12,
+                          "peak_tflops": fp64, "frac": 2.0 * alg * mnk / t / 1e12 / fp64,
+                          "madds_per_mnk": {"algorithmic": alg, "executed": exe},
+                          "peak_kind": "cuBLAS DGEMM rate measured in this run"}
+        pl = block["plain"]
+        pl["roofline"] = {"bound": "fp64 CUDA cores (DGEMM-rate proxy)",
+                          "achieved_tops": PLAIN_OPS[P] * pl["gflops"] / 2.0 / 1e3,
+                          "proxy_peak_tflops": fp64,
+                          "frac_of_proxy": PLAIN_OPS[P] * pl["gflops"] / 2.0 / 1e3 / fp64,
+                          "note": f"{PLAIN_OPS[P]} FP64 operations per multiply-add (the "
+                                  "reference's count, TCtest.cu:136-148), issued as unfused "
+                                  "mul/add; the DGEMM flop rate stands in for the FP64 "
+                                  "CUDA-core peak, which the peaks file does not hold"}
+        sl = block["slice_bf16"]
+        block["slice_over_fp64split"] = {
+            "ratio": sl["gflops"] / sp["gflops"],
+            "equal_accuracy": False,
+            "error_bits_normwise": {"slice_bf16": sl["error_bits_normwise"],
+                                    "fp64split": sp["error_bits_normwise"],
+                                    "plain": pl["error_bits_normwise"]},
+            "note": "not an equal-accuracy ratio: the FP64 split form (the reference's "
+                    "method, 4 slices of 13 bits per limb, truncated convolution) reaches "
+                    "fewer bits than both other forms on these inputs"}
+        block["slice_over_plain"] = sl["gflops"] / pl["gflops"]
+        forms[wl] = block
+        del dA, dB
+        torch.cuda.empty_cache()
+    # hexa-double: the BF16 form (108 digits, 5886 digit pairs) against the
+    # plain hd GEMM on a 1024 x 1024 x 512 problem (uniform inputs, seed 16)
+    rng = np.random.default_rng(16)
+    m, n, k = 1024, 1024, 512
+    A = inputs.uniform_pd(rng, (m, k), 16)
+    B = inputs.uniform_pd(rng, (k, n), 16)
+    dA, dB = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    sample = (range(0, m, 256), range(0, n, 256))
+    hd = {"workload": f"hd {m}x{n}x{k}, hi limbs U[-1,1), seed 16"}
+    hd["slice_bf16"] = bench_form_line(api, ex, stream, 16, A, B, "slice_bf16", dA, dB, sample,
+                                       iters=2)
+    hd["plain"] = bench_form_line(api, ex, stream, 16, A, B, "plain", dA, dB, sample, rows=256)
+    hd["plain"]["rows_timed"] = "rows 0..255 of C (full n, k)"
+    hd["slice_over_plain"] = hd["slice_bf16"]["gflops"] / hd["plain"]["gflops"]
+    forms["hd1024x1024x512"] = hd
+    del dA, dB
+    torch.cuda.empty_cache()
+    # the INT8 tensor rate, against which an int8-digit slice form would
+    # run (cuBLAS through torch._int_mm), beside BF16 at the same size
+    a8 = torch.randint(-128, 127, (8192, 8192), dtype=torch.int8, device="cuda")
+    b8 = a8.t().contiguous().t()
+    a16 = torch.randn(8192, 8192, dtype=torch.bfloat16, device="cuda")
+    torch._int_mm(a8, b8)
+    a16 @ a16
+    t8 = event_time(lambda: torch._int_mm(a8, b8), stream, iters=3)
+    t16 = event_time(lambda: a16 @ a16, stream, iters=3)
+    forms["int8_vs_bf16"] = {"int8_tops": 2.0 * 8192 ** 3 / t8 / 1e12,
+                             "bf16_tflops": 2.0 * 8192 ** 3 / t16 / 1e12,
+                             "how": "torch._int_mm int8 and torch.matmul bf16, 8192^3"}
+    del a8, b8, a16
+    torch.cuda.empty_cache()
+    return forms
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -514,59 +675,7 @@ def main():
 
     forms = None
     if not args.no_forms and rank == 0:
-        forms = {}
-        P2, A2, B2 = inputs.workload("qd1024")
-        dA2, dB2 = torch.from_numpy(A2).cuda(), torch.from_numpy(B2).cuda()
-        r2, c2 = range(0, 1024, 200), range(0, 1024, 200)
-        for form in ("slice_bf16", "fp64split", "plain"):
-            out = torch.empty((1024, 1024, P2), dtype=torch.float64, device="cuda")
-            w2 = torch.empty(max(1, api.workspace_size(form, P2, 1024, 1024, 1024)),
-                             dtype=torch.uint8, device="cuda")
-            api.gemm(dA2, dB2, form, out=out, workspace=w2)
-            t = event_time(lambda: api.gemm(dA2, dB2, form, out=out, workspace=w2), stream,
-                           iters=2 if form == "slice_bf16" else 1)
-            eb = ex.error_bits(out.cpu().numpy(), A2, B2, r2, c2)
-            forms[form] = {"workload": "qd1024", "gflops": 2.0 * 1024 ** 3 / t / 1e9,
-                           "ms": t * 1e3, "error_bits_entrywise": round(eb[0], 1),
-                           "error_bits_normwise": round(eb[1], 1)}
-        if "fp64split" in forms:
-            forms["slice_over_fp64split"] = forms["slice_bf16"]["gflops"] / forms["fp64split"]["gflops"]
-        # FP64 ceiling of the two FP64 forms, measured here (the peaks file
-        # holds BF16 and HBM only): cuBLAS DGEMM through torch.matmul
-        a64 = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
-        torch.matmul(a64, a64)
-        t64 = event_time(lambda: torch.matmul(a64, a64), stream, iters=3)
-        fp64 = 2.0 * 4096 ** 3 / t64 / 1e12
-        del a64
-        forms["fp64_peak"] = {"tflops": fp64, "how": "torch.matmul float64 4096^3 (cuBLAS "
-                              "DGEMM), 3 launches, CUDA events"}
-        # the INT8 tensor rate, against which an int8-digit slice form would
-        # run (cuBLAS through torch._int_mm), beside BF16 at the same size
-        a8 = torch.randint(-128, 127, (8192, 8192), dtype=torch.int8, device="cuda")
-        b8 = a8.t().contiguous().t()
-        a16 = torch.randn(8192, 8192, dtype=torch.bfloat16, device="cuda")
-        torch._int_mm(a8, b8)
-        a16 @ a16
-        t8 = event_time(lambda: torch._int_mm(a8, b8), stream, iters=3)
-        t16 = event_time(lambda: a16 @ a16, stream, iters=3)
-        forms["int8_vs_bf16"] = {"int8_tops": 2.0 * 8192 ** 3 / t8 / 1e12,
-                                 "bf16_tflops": 2.0 * 8192 ** 3 / t16 / 1e12,
-                                 "how": "torch._int_mm int8 and torch.matmul bf16, 8192^3"}
-        del a8, b8, a16
-        mnk = 1024.0 ** 3
-        # split form: per (row, column, k) the DMMA chunks of the 16 output
-        # slices hold sum_i 4 ceil((i + 1) / 4) = 160 multiply-adds
-        sp = 2.0 * 160 * mnk / (forms["fp64split"]["ms"] / 1e3) / 1e12
-        forms["fp64split"]["roofline"] = {"bound": "fp64 tensor (DMMA)", "achieved_tflops": sp,
-                                          "peak_tflops": fp64, "frac": sp / fp64}
-        # plain form: 425 FP64 operations per quad-double multiply-add (the
-        # reference's count, TCtest.cu:136-148), each its own instruction
-        pl = 425.0 * mnk / (forms["plain"]["ms"] / 1e3) / 1e12
-        forms["plain"]["roofline"] = {"bound": "fp64 CUDA cores", "achieved_tflops": pl,
-                                      "peak_tflops": fp64, "frac": pl / fp64,
-                                      "note": "425 FP64 operations per qd multiply-add "
-                                              "(TCtest.cu:136-148), issued as unfused mul/add, "
-                                              "against the DGEMM flop rate"}
+        forms = bench_forms(api, inputs, ex, stream)
 
     batched = None
     if not args.no_forms and rank == 0:
@@ -576,21 +685,24 @@ def main():
     if not args.no_cpu and rank == 0:
         v, sample, _ = cpu_sample(P, A, B, 6.0, os.cpu_count() or 1)
         cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": sample,
+               "sample": sample, "extrapolated": True,
+               "extrapolation": "rate of the row sample at full k; the whole workload at "
+                                f"this rate would take {flops / v / 1e9 / 3600:.0f} h",
                "cudant_conv": cpu_cudant_sample(P, A, B) if P <= 4 else None}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": f"f64x{P} (P-double result) from exact bf16 digit products",
+            "dtype_note": "the arithmetic is exact: 8-bit digits in BF16, FP32 tensor-core "
+                          "sums flushed to int32 before they exceed 2^24, FP64/int64 "
+                          "renormalisation; the error bits below exceed the plain "
+                          "P-double GEMM's",
+            "form": "slice_bf16",
             "data": "synthetic (seeded numpy generators, shapes/distributions of the workload)",
-            "config": {"workload": args.workload, "p": P, "m": m, "n": n, "k": k, "slices": s,
-                       "diagonals": D, "digit_pairs": pairs, "form": "slice_bf16",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": f"inputs (A {A.nbytes / 2**30:.2f} GiB, B {B.nbytes / 2**30:.2f} "
-                             f"GiB, digit planes {2 * s * m * k * 2 / 1e9:.1f} GB) larger "
-                             "than L2 (129 MB), no flush"},
+            "config": bench_config(args.workload, world),
             "e2e": {"value": flops * world / t_e2e / 1e9, "unit": UNIT,
                     "h2d_bytes_per_step": A.nbytes + B.nbytes,
                     "d2h_bytes_per_step": m * n * P * 8,
@@ -600,14 +712,21 @@ def main():
                     "h2d_gbs_first_copy": A.nbytes / t_h2d_first / 1e9,
                     "pipelined_value": flops * world / pipe / 1e9,
                     "pipelined": "mdg_gemm on two device buffer sets; H2D of step i+1 and D2H of step i on copy streams overlap the GEMM of step i"},
-            "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_sust,
-                         "unit": "TFLOP/s", "frac": achieved / bf16_sust,
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_burst,
+                         "unit": "TFLOP/s", "frac": achieved / bf16_burst,
+                         "frac_sustained": achieved / bf16_sust,
+                         "frac_at_max_clock": (achieved * clk["sm_max_mhz"] / clk["sm_mhz"]
+                                               / bf16_burst) if clk.get("sm_mhz") else None,
+                         "clock_note": "frac_at_max_clock scales the achieved rate by "
+                                       "sm_max_mhz / the median SM clock sampled over the "
+                                       "timed steps (the kernel is 95 % of a step)",
                          "traffic": DIAG_TRAFFIC_BYTES.get(args.workload),
                          "traffic_note": "DRAM bytes per launch, one-pass ncu capture of this "
                                          "workload (null where none was taken)",
                          "kernel": "diag_gemm", "kernel_ms": t_diag * 1e3,
                          "algorithmic_tflop_per_launch": tflop,
-                         "peak_kind": f"{peak_kind} bf16 sustained"},
+                         "peak_kind": f"{peak_kind} bf16 burst (frac_sustained: against "
+                                      "the sustained figure)"},
             "gpu_launches": 8 * args.steps,
             "clocks": clk,
             "error_bits": {"slice_bf16": [round(x, 1) for x in bits["slice_bf16"]],

@@ -8,7 +8,15 @@
  * (the reference needs n % nfrag == 0, nfrag <= 32), pllsqueeze_old
  * accepts any n (the reference needs 64 | n when n >= 64), and the
  * dispatchers return zeros for an unsupported p instead of falling off the
- * end of the function.
+ * end of the function.  Every CUDA status is checked: a failed allocation,
+ * copy or launch returns the zero result (t_CUDA = 0) that the reference
+ * returns for an unsupported p.
+ *
+ * The exported kernels keep the reference's launch contract: no bounds
+ * checks, so a launch must cover exactly the entries (ddmm..hdmm: an n x n
+ * grid of threads, r = blockIdx.x * blockDim.x + threadIdx.x, c from y;
+ * renormA / renormbigA: one block of n x n threads; the squeeze kernels:
+ * exactly one thread per entry, with y holding the starting values).
  */
 #ifndef MDG_DROPIN_TCCUDA_H
 #define MDG_DROPIN_TCCUDA_H

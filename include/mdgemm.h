@@ -163,9 +163,12 @@ void mdg_batch_destroy(mdg_batch batch);
  * (64 MiB) inside the library, held on every GPU that loads it; a problem
  * whose BF16 workspace (mdg_gemm_workspace_size) is larger gets
  * MDG_ERROR_TOO_LARGE (e.g. quad-double fits up to 512^3, octo-double up to
- * 256^3).  The first call on a device looks up the array's device address
- * and should come before any stream capture.  Calls share the array: calls
- * that overlap on the GPU race, so order them on one stream. */
+ * 256^3).  The first call in a CUDA context (the device's primary context,
+ * or one the caller made current) looks up the array's device address and
+ * should come before any stream capture; a context created later, e.g.
+ * after cudaDeviceReset, gets its own lookup.  Calls share the array and it
+ * keeps the last call's contents (each call writes every region it reads):
+ * calls that overlap on the GPU race, so order them on one stream. */
 size_t mdg_static_scratch_bytes(void);
 int mdg_gemm_slice_static(int p, int m, int n, int k, const double *A, int lda,
                           const double *B, int ldb, double *C, int ldc,

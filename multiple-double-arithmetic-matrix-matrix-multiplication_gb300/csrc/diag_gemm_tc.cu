@@ -840,15 +840,17 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  // looked up once per process; the initialisation of a function-local
+  // static is serialised between threads
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     void *p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
                                          &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
+      return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    return static_cast<PFN_cuTensorMapEncodeTiled_v12000>(nullptr);
+  }();
   return fn;
 }
 
@@ -884,18 +886,16 @@ int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, co
   CUtensorMap ma, mb;
   MDG_TRY(make_map(&ma, dA, Kp, (long long)s * Mp, TM));
   MDG_TRY(make_map(&mb, dB, Kp, (long long)s * Np, pair ? BH : TN));
-  static int configured_dev[2] = {-1, -1};
   int dev = 0, sms = 0;
   MDG_TRY_CUDA(cudaGetDevice(&dev));
-  if (configured_dev[pair] != dev) {
-    if (pair)
-      MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc2_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
-    else
-      MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    configured_dev[pair] = dev;
-  }
+  // per-device attribute, set on every launch (no process-wide record that
+  // a second device or a second host thread could find stale)
+  if (pair)
+    MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc2_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
+  else
+    MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
   MDG_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   if (pair) {
     const int tiles = (Mp / 256) * (Np / TN2);
@@ -960,14 +960,10 @@ int encode_plane_map(void *map128, const void *base, int Kp, long long rows_tota
 int launch_diag_gemm_grouped(const GroupedProblem *dev_probs, int count, int total_tiles,
                              cudaStream_t st) {
   if (total_tiles == 0) return MDG_SUCCESS;
-  static int configured_dev = -1;
   int dev = 0, sms = 0;
   MDG_TRY_CUDA(cudaGetDevice(&dev));
-  if (configured_dev != dev) {
-    MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc_grouped_kernel,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    configured_dev = dev;
-  }
+  MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc_grouped_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
   MDG_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int grid = total_tiles < sms ? total_tiles : sms;
   diag_gemm_tc_grouped_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(dev_probs, count, total_tiles);

@@ -6,13 +6,17 @@
 // Behaviour kept from the reference: argument order and meaning, the
 // sequence of rand() calls of mat/random_pd (so srand(s) gives the same
 // matrices), reference-compatible slices in split4pd/split8pd/mixsplit2,
-// zeros for an unsupported p in matmulTCnt and pllsqueeze_old.
+// zeros for an unsupported p in matmulTCnt and pllsqueeze_old, extended to
+// every failure: a device allocation, copy or launch that fails gives the
+// zero result (and t_CUDA = 0), with the CUDA error text kept for
+// mdg_last_cuda_error().
 // Behaviour changed: device memory is freed; any n is accepted where the
 // reference needs n % nfrag == 0 or 64 | n; the pllsqueeze / pllntsqueeze
 // dispatchers return zeros for an unsupported p (the reference has no
 // return statement on that path, TCcuda.cu:810-853); a vector shorter than
 // its n x n x p (or planes) shape gives the empty / zero result instead of
 // a read past its end, on the host or, through the device copies, on the GPU.
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 
@@ -32,6 +36,45 @@ struct DevBuf {
   }
 };
 
+// The call succeeded; otherwise its error is recorded (mdg_last_cuda_error).
+bool cuda_ok(cudaError_t e) {
+  if (e == cudaSuccess) return true;
+  mdgi::set_cuda_error(e);
+  return false;
+}
+
+bool to_device(double *dst, const vector<double> &src, size_t count) {
+  return count == 0 ||
+         cuda_ok(cudaMemcpy(dst, src.data(), count * sizeof(double), cudaMemcpyHostToDevice));
+}
+
+// Copies count doubles back; on failure the host vector is cleared to zeros
+// (the reference's result for a call that did not run).
+bool to_host(vector<double> &dst, const double *src, size_t count) {
+  if (count == 0) return true;
+  if (cuda_ok(cudaMemcpy(dst.data(), src, count * sizeof(double), cudaMemcpyDeviceToHost)))
+    return true;
+  std::fill(dst.begin(), dst.end(), 0.0);
+  return false;
+}
+
+// Two events on the legacy default stream around the work of a wrapper;
+// elapsed() is the time between them in ms, or a failure.
+struct Timer {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  bool ok = false;
+  Timer() { ok = cuda_ok(cudaEventCreate(&e0)) && cuda_ok(cudaEventCreate(&e1)); }
+  ~Timer() {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  }
+  bool start() { return ok && cuda_ok(cudaEventRecord(e0)); }
+  bool stop(float &ms) {
+    return cuda_ok(cudaEventRecord(e1)) && cuda_ok(cudaEventSynchronize(e1)) &&
+           cuda_ok(cudaEventElapsedTime(&ms, e0, e1));
+  }
+};
+
 // v holds at least `count` doubles (a negative count never fits)
 bool holds(const vector<double> &v, long long count) {
   return count >= 0 && v.size() >= (size_t)count;
@@ -47,10 +90,9 @@ vector<double> gpu_split(int kind, vector<double> x, int p) {
   vector<double> out((size_t)count * pp, 0.0);
   if (!count) return out;
   DevBuf dx(x.size()), dout(out.size());
-  if (!dx.p || !dout.p) return out;
-  cudaMemcpy(dx.p, x.data(), x.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (!dx.p || !dout.p || !to_device(dx.p, x, x.size())) return out;
   if (mdg_split(kind, 0, p, count, dx.p, dout.p, nullptr) == MDG_SUCCESS)
-    cudaMemcpy(out.data(), dout.p, out.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    to_host(out, dout.p, out.size());
   return out;
 }
 
@@ -338,6 +380,8 @@ __global__ void odmm(double *A, double *B, double *C, int n) { plain_entry<8>(A,
 __global__ void hdmm(double *A, double *B, double *C, int n) { plain_entry<16>(A, B, C, n); }
 
 // matmulTCnt: the plain form on the GPU, loop_ct launches timed with events.
+// Any failure (allocation, copy, launch) returns zeros and t_CUDA = 0, the
+// reference's result when no kernel ran (TCcuda.cu:269-298).
 vector<double> matmulTCnt(vector<double> A, vector<double> B, int n, int nfrag, int p,
                           int loop_ct, float &t_CUDA) {
   (void)nfrag;  // the tiling is the library's; any n works
@@ -348,24 +392,22 @@ vector<double> matmulTCnt(vector<double> A, vector<double> B, int n, int nfrag, 
   if (!holds(A, nnp(n, p)) || !holds(B, nnp(n, p))) return C;
   DevBuf dA(sz), dB(sz), dC(sz);
   if (!dA.p || !dB.p || !dC.p) return C;
-  cudaMemcpy(dA.p, A.data(), sz * sizeof(double), cudaMemcpyHostToDevice);
-  cudaMemcpy(dB.p, B.data(), sz * sizeof(double), cudaMemcpyHostToDevice);
-  cudaMemset(dC.p, 0, sz * sizeof(double));
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventRecord(e0);
-  for (int l = 0; l < loop_ct; ++l)
-    mdg_gemm(MDG_FORM_PLAIN, p, n, n, n, dA.p, n, dB.p, n, dC.p, n, nullptr, nullptr, 0, nullptr);
-  cudaEventRecord(e1);
-  cudaEventSynchronize(e1);
-  cudaEventElapsedTime(&t_CUDA, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaMemcpy(C.data(), dC.p, sz * sizeof(double), cudaMemcpyDeviceToHost);
+  if (!to_device(dA.p, A, sz) || !to_device(dB.p, B, sz) ||
+      !cuda_ok(cudaMemset(dC.p, 0, sz * sizeof(double))))
+    return C;
+  Timer tm;
+  float ms = 0.0f;
+  if (!tm.start()) return C;
+  int st = MDG_SUCCESS;
+  for (int l = 0; l < loop_ct && st == MDG_SUCCESS; ++l)
+    st = mdg_gemm(MDG_FORM_PLAIN, p, n, n, n, dA.p, n, dB.p, n, dC.p, n, nullptr, nullptr, 0,
+                  nullptr);
+  if (!tm.stop(ms) || st != MDG_SUCCESS || !to_host(C, dC.p, sz)) return C;
+  t_CUDA = ms;
   return C;
 }
 
+// The same contract for any form: zeros and t_CUDA = 0 on a failure.
 vector<double> matmulTC(vector<double> A, vector<double> B, int n, int p, int form,
                         const mdg_options *opt, float &t_CUDA) {
   vector<double> C = zeros(n, n, p);
@@ -374,25 +416,18 @@ vector<double> matmulTC(vector<double> A, vector<double> B, int n, int p, int fo
   const size_t sz = (size_t)n * n * p;
   if (!holds(A, nnp(n, p)) || !holds(B, nnp(n, p))) return C;
   DevBuf dA(sz), dB(sz), dC(sz);
+  if (!dA.p || !dB.p || !dC.p) return C;
   const size_t ws_bytes = mdg_gemm_workspace_size(form, p, n, n, n, opt);
-  void *ws = nullptr;
-  if (ws_bytes && cudaMalloc(&ws, ws_bytes) != cudaSuccess) return C;
-  if (dA.p && dB.p && dC.p) {
-    cudaMemcpy(dA.p, A.data(), sz * sizeof(double), cudaMemcpyHostToDevice);
-    cudaMemcpy(dB.p, B.data(), sz * sizeof(double), cudaMemcpyHostToDevice);
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventRecord(e0);
-    const int st = mdg_gemm(form, p, n, n, n, dA.p, n, dB.p, n, dC.p, n, opt, ws, ws_bytes, nullptr);
-    cudaEventRecord(e1);
-    cudaEventSynchronize(e1);
-    cudaEventElapsedTime(&t_CUDA, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (st == MDG_SUCCESS) cudaMemcpy(C.data(), dC.p, sz * sizeof(double), cudaMemcpyDeviceToHost);
-  }
-  if (ws) cudaFree(ws);
+  DevBuf ws((ws_bytes + sizeof(double) - 1) / sizeof(double));
+  if (ws_bytes && !ws.p) return C;
+  if (!to_device(dA.p, A, sz) || !to_device(dB.p, B, sz)) return C;
+  Timer tm;
+  float ms = 0.0f;
+  if (!tm.start()) return C;
+  const int st = mdg_gemm(form, p, n, n, n, dA.p, n, dB.p, n, dC.p, n, opt, ws.p, ws_bytes,
+                          nullptr);
+  if (!tm.stop(ms) || st != MDG_SUCCESS || !to_host(C, dC.p, sz)) return C;
+  t_CUDA = ms;
   return C;
 }
 
@@ -425,19 +460,13 @@ vector<double> pllsqueeze_old(vector<double> x, int p, int pp, float &t_CUDA) {
   vector<double> y = zeros((int)n, 1, mdgi::valid_p(p) ? p : 1);
   if (!mdgi::valid_p(p) || n == 0) return y;
   DevBuf dx(x.size()), dy(y.size());
-  if (!dx.p || !dy.p) return y;
-  cudaMemcpy(dx.p, x.data(), x.size() * sizeof(double), cudaMemcpyHostToDevice);
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventRecord(e0);
+  if (!dx.p || !dy.p || !to_device(dx.p, x, x.size())) return y;
+  Timer tm;
+  float ms = 0.0f;
+  if (!tm.start()) return y;
   const int st = mdg_squeeze(p, pp, n, dx.p, dy.p, nullptr);
-  cudaEventRecord(e1);
-  cudaEventSynchronize(e1);
-  cudaEventElapsedTime(&t_CUDA, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (st == MDG_SUCCESS) cudaMemcpy(y.data(), dy.p, y.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  if (!tm.stop(ms) || st != MDG_SUCCESS || !to_host(y, dy.p, y.size())) return y;
+  t_CUDA = ms;
   return y;
 }
 
@@ -529,10 +558,9 @@ vector<double> gpu_plane_conv(const vector<double> &A, const vector<double> &B, 
   if (!holds(A, (long long)pp * m * k) || !holds(B, (long long)pp * k * n)) return C;
   DevBuf dA(A.size()), dB(B.size()), dC(C.size());
   if ((A.size() && !dA.p) || (B.size() && !dB.p) || !dC.p) return C;
-  cudaMemcpy(dA.p, A.data(), A.size() * sizeof(double), cudaMemcpyHostToDevice);
-  cudaMemcpy(dB.p, B.data(), B.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (!to_device(dA.p, A, A.size()) || !to_device(dB.p, B, B.size())) return C;
   if (mdg_plane_conv(pp, m, n, k, dA.p, dB.p, dC.p, nullptr) == MDG_SUCCESS)
-    cudaMemcpy(C.data(), dC.p, C.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    to_host(C, dC.p, C.size());
   return C;
 }
 
@@ -545,11 +573,10 @@ vector<double> split4pd(vector<double> x) {
   vector<double> out((size_t)count * 4, 0.0);
   if (!count) return out;
   DevBuf dx(x.size()), dout(out.size());
-  if (!dx.p || !dout.p) return out;
-  cudaMemcpy(dx.p, x.data(), x.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (!dx.p || !dout.p || !to_device(dx.p, x, x.size())) return out;
   // one double per entry (P = 1): the slices of each double on its own
   if (mdgi::launch_split(3, 0, 1, count, dx.p, dout.p, 0, 0, nullptr) == MDG_SUCCESS)
-    cudaMemcpy(out.data(), dout.p, out.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    to_host(out, dout.p, out.size());
   return out;
 }
 

@@ -11,14 +11,19 @@
 // The array is a file-scope __device__ variable, so every GPU on which the
 // library is loaded holds its kStaticScratchBytes until the process exits.
 // Host code cannot use the array's name as a device address; the first call
-// on each device looks the address up with cudaGetSymbolAddress (with that
-// device current) and caches it, so that first call should come before any
-// stream capture.  All calls share the array and it keeps the previous
-// call's contents: every region the pipeline reads is written first (the
-// row / column maxima are cleared, digit planes are written in full
-// including padding, every chunk plane is written by the diagonal GEMM), and
-// calls that overlap on the GPU race on the array, so a caller must order
-// them (one stream, or events).
+// in each CUDA context (normally the device's primary context) looks the
+// address up with cudaGetSymbolAddress, with that context current, and
+// caches it under the context's unique id, so that first call should come
+// before any stream capture.  A context created later (after
+// cudaDeviceReset, or a driver-API context the caller makes current) has its
+// own id and gets its own lookup.  All calls share the array and it keeps
+// the previous call's contents: every region the pipeline reads is written
+// first (the row / column maxima are cleared, digit planes are written in
+// full including padding, every chunk plane is written by the diagonal
+// GEMM), and calls that overlap on the GPU race on the array, so a caller
+// must order them (one stream, or events).
+#include <cuda.h>
+
 #include <mutex>
 
 #include "common.cuh"
@@ -27,26 +32,63 @@
 namespace {
 
 constexpr size_t kStaticScratchBytes = 64ull << 20;  // 64 MiB per device
-constexpr int kMaxDevices = 64;
+constexpr int kMaxContexts = 64;
 
 __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
-std::mutex g_mu;
-void *g_scratch_ptr[kMaxDevices] = {};
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
 
-// Device address of the scratch array on the current device (looked up once
-// per device with that device current).
+template <typename Fn>
+Fn driver_entry(const char *name, int version) {
+  void *p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &p, version, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    return reinterpret_cast<Fn>(p);
+  return nullptr;
+}
+
+// Unique id of the current context (0 when none is current yet).
+int current_context_id(unsigned long long *id) {
+  static const CtxGetCurrentFn get_current = driver_entry<CtxGetCurrentFn>("cuCtxGetCurrent", 4000);
+  static const CtxGetIdFn get_id = driver_entry<CtxGetIdFn>("cuCtxGetId", 12000);
+  if (!get_current || !get_id) return MDG_ERROR_NOT_SUPPORTED;
+  CUcontext ctx = nullptr;
+  *id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS) return MDG_ERROR_CUDA;
+  if (ctx && get_id(ctx, id) != CUDA_SUCCESS) return MDG_ERROR_CUDA;
+  return MDG_SUCCESS;
+}
+
+std::mutex g_mu;
+struct Entry {
+  unsigned long long ctx;
+  void *ptr;
+};
+Entry g_entries[kMaxContexts] = {};
+int g_next = 0;
+
+// Device address of the scratch array in the current context.
 int scratch_address(void **out) {
-  int dev = 0;
-  MDG_TRY_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return MDG_ERROR_NOT_SUPPORTED;
+  unsigned long long id = 0;
+  MDG_TRY(current_context_id(&id));
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_ptr[dev]) {
-    void *p = nullptr;
-    MDG_TRY_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
-    g_scratch_ptr[dev] = p;
-  }
-  *out = g_scratch_ptr[dev];
+  if (id)
+    for (const Entry &e : g_entries)
+      if (e.ctx == id) {
+        *out = e.ptr;
+        return MDG_SUCCESS;
+      }
+  // first call in this context: the runtime call below also makes the
+  // device's primary context current when no context was
+  void *p = nullptr;
+  MDG_TRY_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
+  MDG_TRY(current_context_id(&id));
+  if (!id) return MDG_ERROR_CUDA;
+  g_entries[g_next] = Entry{id, p};
+  g_next = (g_next + 1) % kMaxContexts;
+  *out = p;
   return MDG_SUCCESS;
 }
 

@@ -65,12 +65,10 @@ template <int P>
 int launch(int m, int n, int k, const double *A, int lda, const double *B, int ldb, double *C,
            int ldc, cudaStream_t st) {
   const size_t smem = 2 * T * T * P * sizeof(double);
-  static bool configured = false;
-  if (!configured) {
-    MDG_TRY_CUDA(cudaFuncSetAttribute(plain_gemm_kernel<P>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured = true;
-  }
+  // the attribute belongs to the current device: set it on every launch
+  // (a host-side call of about a microsecond) rather than remember it
+  MDG_TRY_CUDA(cudaFuncSetAttribute(plain_gemm_kernel<P>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid(mdgi::ceil_div(n, T), mdgi::ceil_div(m, T)), block(T, T);
   plain_gemm_kernel<P><<<grid, block, smem, st>>>(m, n, k, A, lda, B, ldb, C, ldc);
   MDG_TRY_LAUNCH();

@@ -1,6 +1,11 @@
-"""The drop-in C++ surface on the host (no GPU): a small C++ program linked
-against libmdgemm.so runs the reference-named host functions and the
-results are compared with the golden vectors made by the reference itself.
+"""The drop-in C++ surface: a small C++ program linked against libmdgemm.so
+runs the reference-named functions and the results are compared with the
+golden vectors made by the reference itself.  The host functions are tested
+without a GPU; the tests marked gpu run the std::vector wrappers
+(matmulTCnt, matmulTC, split4pd / split8pd / mixsplit2, pllsqueeze_old,
+pllsqueeze, pllsqueeze_2_{8,12,16}) and launch every kernel TCcuda.h
+exports (ddmm..hdmm, renormA, renormbigA, pllsqueeze_{2,4,8,16}_pp_old,
+pllsqueeze_kernel_2_{8,12,16}) the way the reference's code does.
 Also checks that the reference's own driver compiles against the drop-in
 headers when the reference sources are present."""
 import os
@@ -24,14 +29,17 @@ def prog(tmp_path_factory):
     libdir = os.path.dirname(lib)
     subprocess.run([NVCC, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
                     "-x", "cu", os.path.join(ROOT, "tests", "cpp", "test_dropin.cpp"),
-                    "-gencode", "arch=compute_103a,code=sm_103a",
+                    "-gencode", "arch=compute_103a,code=sm_103a", "-cudart", "shared",
                     "-L", libdir, "-lmdgemm", "-Xlinker", "-rpath," + libdir, "-o", out],
                    check=True, capture_output=True)
     return out
 
 
 def run(prog, *args):
-    subprocess.run([prog] + [str(a) for a in args], check=True, capture_output=True, timeout=120)
+    r = subprocess.run([prog] + [str(a) for a in args], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, (args[:3], r.returncode, r.stderr[-2000:])
+    return r.stdout
 
 
 def test_mat_reproduces_reference_rand_sequence(prog, tmp_path):
@@ -136,3 +144,146 @@ def test_reference_driver_compiles_against_dropin_headers(tmp_path):
                         "-L", libdir, "-lmdgemm", "-o", str(tmp_path / "mytest")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+# ------------------------------------------------------------------ GPU --
+
+def _roundtrip(prog, tmp_path, args, inputs, out_shape=None):
+    """Write the inputs, run the command with their paths, read the output."""
+    paths = []
+    for i, x in enumerate(inputs):
+        path = tmp_path / f"in{i}.bin"
+        np.ascontiguousarray(x, dtype=np.float64).tofile(path)
+        paths.append(path)
+    out = tmp_path / "out.bin"
+    run(prog, *args, *paths, out)
+    got = np.fromfile(out)
+    return got.reshape(out_shape) if out_shape is not None else got
+
+
+GOLDEN_MATMUL = [(2, "matmul_P2"), (4, "matmul_P4"), (8, "matmul_P8"), (16, "matmul_P16"),
+                 (2, "matmul_dd64")]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("P,name", GOLDEN_MATMUL)
+def test_gpu_matmulTCnt_wrapper_matches_reference(prog, tmp_path, P, name):
+    """matmulTCnt (TCcuda.cu:248-302) through the std::vector wrapper:
+    the reference's host product bit for bit, two timed launches."""
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    n = g["A"].shape[0]
+    got = _roundtrip(prog, tmp_path, ["tcnt", P, n, min(32, n)], [g["A"], g["B"]],
+                     g["C"].shape)
+    assert np.array_equal(got, g["C"], equal_nan=True)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("P,name", GOLDEN_MATMUL)
+def test_gpu_exported_plain_kernels_match_reference(prog, tmp_path, P, name):
+    """ddmm / qdmm / odmm / hdmm launched by the caller as matmulTCnt does in
+    the reference (grid (n/nfrag)^2, block nfrag^2, TCcuda.cu:262-297)."""
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    n = g["A"].shape[0]
+    nfrag = 32 if n % 32 == 0 else n
+    got = _roundtrip(prog, tmp_path, ["kmm", P, n, nfrag], [g["A"], g["B"]], g["C"].shape)
+    assert np.array_equal(got, g["C"], equal_nan=True)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("P", [2, 4, 8])
+def test_gpu_matmulTC_wrapper_all_forms(prog, tmp_path, orc, inputs, P):
+    """matmulTC in the plain (bit for bit), FP64-split (oracle error bits
+    within 2) and BF16 slice (bit for bit vs the oracle) forms."""
+    ex = pkg("errors")
+    n = 24
+    rng = np.random.default_rng(P + 40)
+    A = inputs.uniform_pd(rng, (n, n), P)
+    B = inputs.uniform_pd(rng, (n, n), P)
+    plain = _roundtrip(prog, tmp_path, ["tc", 0, P, n], [A, B], (n, n, P))
+    assert np.array_equal(plain, orc.gemm_plain(P, A, B, n, n, n))
+    s = pkg("api").default_slices(P)
+    sl = _roundtrip(prog, tmp_path, ["tc", 2, P, n], [A, B], (n, n, P))
+    assert np.array_equal(sl, orc.gemm_slices(P, s, s, A, B, n, n, n))
+    sp = _roundtrip(prog, tmp_path, ["tc", 1, P, n], [A, B], (n, n, P))
+    ref = orc.gemm_fp64split(P, A, B, n, n, n)
+    bits = ex.error_bits(sp, A, B, range(n), range(n))
+    bits_ref = ex.error_bits(ref, A, B, range(n), range(n))
+    assert bits[1] >= bits_ref[1] - 2.0, (bits, bits_ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("P", [2, 4, 8, 16])
+@pytest.mark.parametrize("kind", ["split4", "split8"])
+@pytest.mark.parametrize("style", ["", "_refstyle"])
+def test_gpu_split_wrappers_match_reference(prog, tmp_path, P, kind, style):
+    """split4pd / split8pd (floatybits.cu:515,622) through the wrapper."""
+    g = np.load(os.path.join(GOLDEN, f"{kind}_P{P}{style}.npz"))
+    got = _roundtrip(prog, tmp_path, ["gsplit", kind, P], [g["x"]], g["out"].shape)
+    assert np.array_equal(got, g["out"])
+    assert np.array_equal(np.signbit(got), np.signbit(g["out"]))
+
+
+@pytest.mark.gpu
+def test_gpu_mixsplit2_wrapper_matches_reference(prog, tmp_path):
+    g = np.load(os.path.join(GOLDEN, "split_mix_P2.npz"))
+    got = _roundtrip(prog, tmp_path, ["gsplit", "mix", 2], [g["x"]], g["out"].shape)
+    assert np.array_equal(got, g["out"])
+    assert np.array_equal(np.signbit(got), np.signbit(g["out"]))
+
+
+SQUEEZES = [(2, 8), (2, 12), (2, 16), (4, 16), (4, 32), (8, 32), (8, 64), (16, 64), (16, 128)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("P,pp", SQUEEZES)
+def test_gpu_squeeze_wrappers_match_reference(prog, tmp_path, P, pp):
+    """pllsqueeze_old and pllsqueeze (TCcuda.cu:908, 810) through the
+    wrappers; for double-double also pllsqueeze_2_{8,12,16} (TCcuda.cu:412)."""
+    g = np.load(os.path.join(GOLDEN, f"squeeze_P{P}_pp{pp}.npz"))
+    hows = ["old", "any"] + (["dd"] if P == 2 else [])
+    for how in hows:
+        got = _roundtrip(prog, tmp_path, ["gsqueeze", how, P, pp], [g["x"]], g["y"].shape)
+        assert np.array_equal(got, g["y"]), how
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("P,pp", SQUEEZES)
+def test_gpu_exported_squeeze_kernels_match_reference(prog, tmp_path, P, pp):
+    """pllsqueeze_{2,4,8,16}_pp_old (TCcuda.cu:876-906) launched by the caller
+    with exactly one thread per entry."""
+    g = np.load(os.path.join(GOLDEN, f"squeeze_P{P}_pp{pp}.npz"))
+    count = g["x"].shape[0]
+    got = _roundtrip(prog, tmp_path, ["ksqpp", P, pp, count // 16, 16], [g["x"]], g["y"].shape)
+    assert np.array_equal(got, g["y"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pp", [8, 12, 16])
+def test_gpu_separate_plane_squeeze_kernels(prog, tmp_path, orc, pp):
+    """pllsqueeze_kernel_2_{8,12,16} (TCcuda.cu:400, 508, 646) on the
+    reference's golden partials, and on 1000 entries launched as <<<8, 125>>>
+    (a count that is not a multiple of a power-of-two block), against the
+    oracle's squeeze; these kernels have no bounds check, so the launch
+    covers exactly the entries."""
+    g = np.load(os.path.join(GOLDEN, f"squeeze_P2_pp{pp}.npz"))
+    count = g["x"].shape[0]
+    got = _roundtrip(prog, tmp_path, ["ksq2", pp, count // 16, 16], [g["x"]], g["y"].shape)
+    assert np.array_equal(got, g["y"])
+    rng = np.random.default_rng(pp)
+    x = np.ldexp(rng.uniform(-1, 1, size=(1000, pp)), -13 * np.arange(pp))
+    got = _roundtrip(prog, tmp_path, ["ksq2", pp, 8, 125], [x], (1000, 2))
+    assert np.array_equal(got, orc.squeeze(2, pp, x))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("P", [2, 4, 8, 16])
+@pytest.mark.parametrize("which,golden", [("A", "renormhost"), ("bigA", "renormhostbig")])
+def test_gpu_exported_renorm_kernels_match_reference(prog, tmp_path, P, which, golden):
+    """renormA / renormbigA (TCcuda.cu:97-117), one block of n x n threads,
+    against the reference's host renormhost / renormhostbig of the same
+    pass (not an error-free transform; kept as the reference defines it)."""
+    g = np.load(os.path.join(GOLDEN, f"hostfuncs_P{P}.npz"))
+    n = int(g["n"])
+    got = _roundtrip(prog, tmp_path, ["krenorm", which, P, n], [g["A"]])
+    assert np.array_equal(got, g[golden])
+    assert np.array_equal(np.signbit(got), np.signbit(g[golden]))

@@ -156,6 +156,26 @@ def test_fp64split_error_bits(api, orc, inputs, name, P):
     assert bits[1] >= bits_ref[1] - 2.0, (bits, bits_ref)
 
 
+@pytest.mark.parametrize("kind,P", [("split8", 2), ("split8", 4), ("split8", 8), ("mix", 2)])
+def test_fp64split_gemm_other_split_kinds(api, orc, inputs, kind, P):
+    """The split GEMM with the 8-slice split (split8pd, pp = 8P,
+    floatybits.cu:622) and the mixed double-double split (mixsplit2, pp = 12,
+    floatybits.cu:646), the choices of TCtest.cu:53-62: the same bound as
+    the 4-slice form against the oracle's end-to-end split GEMM."""
+    ex = pkg("errors")
+    m, n, k = 20, 18, 33
+    rng = np.random.default_rng(len(kind) * 10 + P)
+    A = inputs.uniform_pd(rng, (m, k), P)
+    B = inputs.uniform_pd(rng, (k, n), P)
+    C = host(api.gemm(dev(A), dev(B), "fp64split", split_kind=kind))
+    ref = orc.gemm_fp64split(P, A, B, m, n, k, kind=kind)
+    bits = ex.error_bits(C, A, B, range(m), range(n))
+    bits_ref = ex.error_bits(ref, A, B, range(m), range(n))
+    assert bits[1] >= bits_ref[1] - 2.0, (bits, bits_ref)
+    norms = np.abs(A[..., 0]) @ np.abs(B[..., 0])
+    assert np.all(np.abs(C[..., 0] - ref[..., 0]) <= 2.0 ** -48 * norms)
+
+
 def test_fp64split_reference_compatible_mode(api, orc, inputs):
     rng = np.random.default_rng(9)
     A = inputs.reference_pd(rng, (16, 16), 4)
@@ -327,6 +347,49 @@ def test_octo_double_referee_agrees_with_exact_product(api, inputs):
     ref = ex.referee_error_bits(C, R, norms)
     assert abs(ref[0] - exact[0]) <= 1.0 and abs(ref[1] - exact[1]) <= 1.0, (ref, exact)
     assert ref[1] > 200
+
+
+def test_two_host_threads_launch_at_once(api, inputs):
+    """Two host threads issue GEMMs at the same time, each on its own
+    stream, mixing the plain form at P = 16 (64 KiB of dynamic shared
+    memory) with the CTA-pair and single-CTA slice engines: every result
+    equals the same call made alone, so the launch path keeps no
+    process-wide state that the threads could race on."""
+    import threading
+    cases = [[(16, 40, 30, 20, "plain", "auto"), (4, 300, 260, 130, "slice_bf16", "tc_pair"),
+              (2, 128, 256, 64, "slice_bf16", "tc")],
+             [(8, 64, 64, 64, "plain", "auto"), (2, 256, 512, 128, "slice_bf16", "tc_pair"),
+              (16, 20, 20, 20, "slice_bf16", "auto")]]
+    rng = np.random.default_rng(77)
+    ops = [[(dev(inputs.uniform_pd(rng, (m, k), P)), dev(inputs.uniform_pd(rng, (k, n), P)))
+            for P, m, n, k, _, _ in row] for row in cases]
+    want = [[host(api.gemm(A, B, c[4], engine=c[5])) for c, (A, B) in zip(row, o)]
+            for row, o in zip(cases, ops)]
+    got = [[None] * len(row) for row in cases]
+    errors = []
+
+    def worker(t):
+        try:
+            s = torch.cuda.Stream()
+            for rep in range(3):
+                for i, (c, (A, B)) in enumerate(zip(cases[t], ops[t])):
+                    C = api.gemm(A, B, c[4], engine=c[5], stream=s)
+                    s.synchronize()
+                    if rep == 2:
+                        got[t][i] = host(C)
+        except Exception as e:  # reported on the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(t,)) for t in range(2)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    for t in range(2):
+        for i in range(len(cases[t])):
+            assert np.array_equal(got[t][i], want[t][i]), (t, i)
+    assert api.device_status() == 0
 
 
 def test_host_entry_matches_device_entry(api, inputs):
