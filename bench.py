@@ -207,6 +207,25 @@ def cpu_cudant_sample(P, A, B, n=256):
             "sample": f"{n}^3 block, {pp} slice planes, manualconvmult order", "seconds": dt}
 
 
+def reference_cpu_sample(P, A, B, threads, nsub):
+    """The reference's own host GEMM (matmul{dd,qd,od}f, TCcuda.cu:320-359,
+    built from its sources into oracle/_ref) on the leading nsub x nsub x nsub
+    block of the workload, one independent copy per host thread (the
+    reference is single-threaded): (md-GFLOP/s, sample text, seconds)."""
+    import concurrent.futures as cf
+
+    import oracle
+    Asub = np.ascontiguousarray(A[:nsub, :nsub])
+    Bsub = np.ascontiguousarray(B[:nsub, :nsub])
+    name = {2: "matmulddf", 4: "matmulqdf", 8: "matmulodf", 16: "matmulhdf"}[P]
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(lambda _: oracle.ref_matmul(P, Asub, Bsub, nsub), range(threads)))
+    dt = time.perf_counter() - t0
+    return (2.0 * nsub ** 3 * threads / dt / 1e9,
+            f"{threads} threads x {name} on the leading {nsub}^3 block (reference sources)", dt)
+
+
 def run_reference(args):
     """The reference's CPU path, timed on the host cores."""
     world, rank = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
@@ -217,23 +236,11 @@ def run_reference(args):
     oracle.build()
     threads = os.cpu_count() or 1
     P, A, B = inputs.workload(args.workload)
-    kind = "port"
-    if oracle.ref_available():
-        kind = "reference"
+    kind = "reference" if oracle.ref_available() else "port"
     vals, times = [], []
     for i in range(args.warmup + args.steps):
         if kind == "reference":
-            # square sub-problem through the reference's matmulqdf, one per thread
-            import concurrent.futures as cf
-            nsub = 96
-            Asub = np.ascontiguousarray(A[:nsub, :nsub])
-            Bsub = np.ascontiguousarray(B[:nsub, :nsub])
-            t0 = time.perf_counter()
-            with cf.ThreadPoolExecutor(threads) as ex:
-                list(ex.map(lambda _: oracle.ref_matmul(P, Asub, Bsub, nsub), range(threads)))
-            dt = time.perf_counter() - t0
-            v = 2.0 * nsub ** 3 * threads / dt / 1e9
-            sample = f"{threads} x matmulqdf n={nsub} (reference sources)"
+            v, sample, dt = reference_cpu_sample(P, A, B, threads, 128 if P <= 4 else 64)
         else:
             v, sample, dt = cpu_sample(P, A, B, 3.0, threads)
         if i >= args.warmup:
@@ -249,7 +256,7 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
                          "sample": sample, "extrapolated": True,
                          "extrapolation": "rate of the sample; the whole workload at this rate "
-                                          f"would take {2.0 * np.prod(inputs.WORKLOADS[args.workload][1:4]) / value / 1e9 / 3600:.0f} h"},
+                                          f"would take {2.0 * np.prod(inputs.WORKLOADS[args.workload][1:4]) / value / 1e9 / 3600:.1f} h"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -683,11 +690,18 @@ def main():
 
     cpu = None
     if not args.no_cpu and rank == 0:
-        v, sample, _ = cpu_sample(P, A, B, 6.0, os.cpu_count() or 1)
-        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+        import oracle
+        threads = os.cpu_count() or 1
+        if oracle.ref_available():
+            v, sample, _ = reference_cpu_sample(P, A, B, threads, 192 if P <= 4 else 96)
+            kind = "reference"
+        else:
+            v, sample, _ = cpu_sample(P, A, B, 6.0, threads)
+            kind = "port"
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": sample, "extrapolated": True,
-               "extrapolation": "rate of the row sample at full k; the whole workload at "
-                                f"this rate would take {flops / v / 1e9 / 3600:.0f} h",
+               "extrapolation": "rate of the sample; the whole workload at "
+                                f"this rate would take {flops / v / 1e9 / 3600:.1f} h",
                "cudant_conv": cpu_cudant_sample(P, A, B) if P <= 4 else None}
 
     if rank == 0:

@@ -22,7 +22,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 _BUILD = os.path.join(HERE, "_build", "liboracle.so")
 _REF = os.path.join(HERE, "_ref", "libref.so")
 _CUDANT = os.path.join(HERE, "_ref", "libcudant.so")
-REF_SOURCES = "/root/reference/C++"
+# the reference's C++ sources, staged beside the repository by `make stage`
+REF_SOURCES = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "C++")
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -31,8 +32,11 @@ _lp = ctypes.POINTER(ctypes.c_int64)
 
 def build(ref=None):
     """Compile oracle.c (and the reference libraries when the reference
-    sources exist and ``ref`` is not False)."""
+    sources exist and ``ref`` is not False).  The sources are staged into
+    REF_SOURCES first when a reference checkout is at hand."""
     targets = ["oracle"]
+    if ref is not False:
+        subprocess.run(["make", "-s", "-C", HERE, "stage"], check=True)
     if ref is None:
         ref = os.path.isdir(REF_SOURCES)
     if ref:

@@ -130,7 +130,40 @@ def test_every_declared_kernel_links(prog):
     assert r.stdout.strip() == "13"
 
 
-REF_DRIVER = "/root/reference/C++/TCtest.cu"
+# the reference's driver, from the sources staged beside the repository
+REF_DRIVER = os.path.join(ROOT, "baseline", "_ref", "C++", "TCtest.cu")
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference sources not present")
+def test_reference_driver_runs_against_the_library(tmp_path):
+    """The reference's driver, unmodified (TCtest.cu:48-208: p = 8, n = 64,
+    q = 4), built against the drop-in headers and libmdgemm.so and run on the
+    GPU: mat, split4pd and bigB2 from the library feed the driver's own wmma
+    DMMA kernel, pllsqueeze_old squeezes its 32 partials per entry and
+    matmulTCnt computes the plain octo-double product.  The driver prints
+    the largest difference of the two results; with its positive inputs of
+    magnitude about 36 both forms are accurate to about 2^-410, so the
+    difference is far below 1e-100."""
+    lib = pkg("_lib").LIB_PATH
+    libdir = os.path.dirname(lib)
+    exe = str(tmp_path / "mytest")
+    r = subprocess.run([NVCC, "-std=c++17", "-w", "-I", os.path.join(ROOT, "include"),
+                        REF_DRIVER, "-gencode", "arch=compute_103a,code=sm_103a",
+                        "-cudart", "shared", "-L", libdir, "-lmdgemm",
+                        "-Xlinker", "-rpath," + libdir, "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    print(r.stdout)
+    lines = dict(line.split("? ", 1) for line in r.stdout.splitlines() if "? " in line)
+    max_err = float(lines["Max error"].split()[0])
+    assert 0.0 <= max_err < 1e-100, r.stdout
+    tc = [float(v) for v in lines["TC C[1,1]"].strip("()").split(",")]
+    plain = [float(v) for v in lines["CUDA C[1,1]"].strip("()").split(",")]
+    assert len(tc) == len(plain) == 8 and 1.0 < tc[0] < 64.0
+    assert abs(tc[0] - plain[0]) <= 1e-13 * plain[0]
 
 
 @pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference sources not present")
