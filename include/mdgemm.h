@@ -142,17 +142,34 @@ void mdg_release_cache(void);
  * out `workspace` (mdg_batch_workspace_size bytes) for these problems
  * (device pointers, P in {2,4,8,16}, m, n, k >= 1, default digits per P),
  * uploads the per-problem tables and tensor maps and returns a handle;
- * it synchronises `stream`.  mdg_batch_run only launches kernels (8 per
- * batch: exponents, digits, one grouped tcgen05 diagonal GEMM over the
- * tiles of every problem, renormalisation) and may be captured into a CUDA
- * graph; each C equals the single-problem mdg_gemm result bit for bit.  No
- * counterpart in the reference. */
+ * it synchronises `stream`.  mdg_batch_run only launches kernels (4 per
+ * batch, whatever the mix of P: exponents of every row and column, digits
+ * of every operand, one grouped tcgen05 diagonal GEMM over the tiles of
+ * every problem, renormalisation of every C) and may be captured into a
+ * CUDA graph; each C equals the single-problem mdg_gemm result bit for bit.
+ * No counterpart in the reference. */
 typedef struct mdg_batch_s *mdg_batch;
 size_t mdg_batch_workspace_size(const mdg_problem *problems, int count);
 int mdg_batch_create(const mdg_problem *problems, int count, void *workspace,
                      size_t workspace_bytes, void *stream, mdg_batch *out);
 int mdg_batch_run(mdg_batch batch, void *stream);
 void mdg_batch_destroy(mdg_batch batch);
+
+/* Tile policies of the batched plan's diagonal GEMM: tiles of 128 rows by
+ * 256 columns only, by 128 columns only, or (auto) 128 columns for the
+ * problems where that pads fewer columns (n mod 256 in 1..128), else 256.
+ * Every policy gives the same bits. */
+enum { MDG_BATCH_TILES_AUTO = 0, MDG_BATCH_TILES_256 = 1, MDG_BATCH_TILES_128 = 2 };
+/* Re-deals the plan's tiles under `policy` (uploads the tile table and
+ * synchronises `stream`; not during a capture).  mdg_batch_tiles returns
+ * the policy in use. */
+int mdg_batch_set_tiles(mdg_batch batch, int policy, void *stream);
+int mdg_batch_tiles(mdg_batch batch);
+/* Times one mdg_batch_run under each tile policy (after a warm-up each),
+ * keeps the fastest and records it in the tuning cache under the batch's
+ * problem shapes; mdg_batch_create starts later plans of the same shapes
+ * with the recorded policy.  Synchronises `stream`. */
+int mdg_batch_tune(mdg_batch batch, void *stream);
 
 /* C = A * B in the BF16 slice-digit form (default digits) without any
  * device allocation and without a workspace argument, for callers that may

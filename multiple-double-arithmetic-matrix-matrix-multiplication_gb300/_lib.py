@@ -73,6 +73,9 @@ SIGNATURES = {
     "mdg_batch_create": (c_int, [_P_PROB, c_int, c_vp, c_size, c_vp, ctypes.POINTER(c_vp)]),
     "mdg_batch_run": (c_int, [c_vp, c_vp]),
     "mdg_batch_destroy": (None, [c_vp]),
+    "mdg_batch_set_tiles": (c_int, [c_vp, c_int, c_vp]),
+    "mdg_batch_tiles": (c_int, [c_vp]),
+    "mdg_batch_tune": (c_int, [c_vp, c_vp]),
     "mdg_gemm_slice_static": (c_int, [c_int] * 4 + [c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp]),
 }
 

@@ -207,6 +207,25 @@ class BatchPlan:
         check(lib().mdg_batch_run(self.handle, _stream(stream)), "mdg_batch_run")
         return self.Cs
 
+    TILES = {"auto": 0, "256": 1, "128": 2}
+
+    @property
+    def tiles(self):
+        """The tile policy in use: "auto", "256" or "128"."""
+        code = lib().mdg_batch_tiles(self.handle)
+        return {v: k for k, v in self.TILES.items()}[code]
+
+    def set_tiles(self, policy, stream=None):
+        """Re-deal the grouped GEMM's tiles (same bits under every policy)."""
+        check(lib().mdg_batch_set_tiles(self.handle, self.TILES[str(policy)], _stream(stream)),
+              "mdg_batch_set_tiles")
+
+    def tune(self, stream=None):
+        """Time every tile policy on the plan's operands, keep the fastest
+        (recorded in the tuning cache for plans of the same shapes)."""
+        check(lib().mdg_batch_tune(self.handle, _stream(stream)), "mdg_batch_tune")
+        return self.tiles
+
     def __del__(self):
         if getattr(self, "handle", None):
             lib().mdg_batch_destroy(self.handle)

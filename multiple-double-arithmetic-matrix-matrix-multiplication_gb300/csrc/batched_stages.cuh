@@ -1,6 +1,11 @@
-// Digit and renormalisation kernels of the batched slice-digit GEMM, one
-// translation unit per integer width (batched_w{4,6,10,16}.cu) so that the
-// wide-integer code compiles in parallel.
+// Exponent, digit and renormalisation kernels of the batched slice-digit
+// GEMM: one launch per stage over every problem of the batch, whatever its
+// P.  Each block finds its problem in the table (batched_table.cuh) and
+// branches on the problem's P to the integer width that P needs; the
+// branches of wider integers than the batch holds are not compiled into
+// the instance that is launched (NWMAX).  One translation unit per NWMAX
+// (batched_w{4,6,10,16}.cu) so that the wide-integer code compiles in
+// parallel.
 #pragma once
 
 #include "batched_table.cuh"
@@ -8,67 +13,134 @@
 
 namespace mdgi {
 
-// Blocks x0 + blockIdx.x of the problems' digit rows (one P group of the
-// table, which the plan sorts by P).
-template <int NW, int Side>
-__global__ void digits_b(const BatchProblem *__restrict__ pr, int count, const int *__restrict__ E,
-                         int x0) {
-  const int x = x0 + (int)blockIdx.x;
-  const int q = find_problem<Side == 0 ? 2 : 3>(pr, count, x);
-  const BatchProblem &b = pr[q];
-  const int pc = blockIdx.y * blockDim.x + threadIdx.x;
-  if (pc >= b.Kp) return;
-  if (Side == 0)
-    mdgi::digits_elem<NW>(b.p, b.s, b.m, b.k, b.A, b.lda, E + b.offE, 0, b.dA, b.Kp, b.plane_a,
-                          b.Mp, b.Kp, x - b.digA_begin, pc);
-  else
-    mdgi::digits_elem<NW>(b.p, b.s, b.n, b.k, b.B, b.ldb, E + b.offF, 1, b.dB, b.Kp, b.plane_b,
-                          b.Np, b.Kp, x - b.digB_begin, pc);
-}
-
-// Output rows x0 + blockIdx.x of one P group, V adjacent columns per thread
-// (chunk planes are Np wide with Np a multiple of 256 and start 256-byte
-// aligned, so V-wide loads stay aligned).
-template <int P, int NW, int V>
-__global__ void __launch_bounds__(128) renorm_b(const BatchProblem *__restrict__ pr, int count,
-                                                const int *__restrict__ E, int x0) {
-  const int x = x0 + (int)blockIdx.x;
-  const int q = find_problem<4>(pr, count, x);
-  const BatchProblem &b = pr[q];
-  const int r = x - b.out_begin, c = (blockIdx.y * blockDim.x + threadIdx.x) * V;
-  mdgi::renorm_elems<P, NW, V>(b.s, b.D, b.Kp / 64, b.m, b.n, b.chunks, b.plane_c, b.Np,
-                               E + b.offE, E + b.offF, b.C, b.ldc, r, c);
-}
-
-template <int NW>
-int launch_batch_digits(const BatchProblem *pr, int count, const int *E, dim3 ga, dim3 gb,
-                        int xa, int xb, cudaStream_t st) {
-  digits_b<NW, 0><<<ga, 128, 0, st>>>(pr, count, E, xa);
-  MDG_TRY_LAUNCH();
-  digits_b<NW, 1><<<gb, 128, 0, st>>>(pr, count, E, xb);
-  MDG_TRY_LAUNCH();
-  return MDG_SUCCESS;
-}
-
-template <int P, int NW>
-int launch_renorm_group(const BatchProblem *pr, int count, const int *E, int rows, int max_n,
-                        int x0, cudaStream_t st) {
-  constexpr int V = NW <= 6 ? 4 : NW <= 10 ? 2 : 1;
-  const dim3 g(rows, ceil_div(ceil_div(max_n, V), 128));
-  renorm_b<P, NW, V><<<g, 128, 0, st>>>(pr, count, E, x0);
-  MDG_TRY_LAUNCH();
-  return MDG_SUCCESS;
-}
-
-template <int NW>
-int launch_batch_renorm(int p, const BatchProblem *pr, int count, const int *E, int rows,
-                        int max_n, int x0, cudaStream_t st) {
-  switch (p) {
-    case 2: return launch_renorm_group<2, NW>(pr, count, E, rows, max_n, x0, st);
-    case 4: return launch_renorm_group<4, NW>(pr, count, E, rows, max_n, x0, st);
-    case 8: return launch_renorm_group<8, NW>(pr, count, E, rows, max_n, x0, st);
-    default: return launch_renorm_group<16, NW>(pr, count, E, rows, max_n, x0, st);
+// Row exponents of A (one warp per row) and column exponents of B (32
+// columns x 8 row groups per block), each from the maximum over the whole
+// row / column of sum_l |x_l| -- the value, order of additions and rounding
+// of the single-problem absmax kernel -- so no atomics and no cleared
+// maxima are needed.  (A template only so that each translation unit
+// holds its own instance.)
+template <int NWMAX>
+__global__ void __launch_bounds__(256)
+    scale_all(const BatchProblem *__restrict__ pr, int count, int *__restrict__ exps) {
+  const int u = blockIdx.x;
+  const BatchProblem &b = pr[find_problem<kScaleUnits>(pr, count, u)];
+  const int lu = u - b.scale_begin;
+  const int P = b.p;
+  if (lu < b.scale_b_off) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = 8 * lu + warp;
+    if (r >= b.m) return;
+    double mx = 0.0;
+    for (int c = lane; c < b.k; c += 32) {
+      const double *x = b.A + ((size_t)r * b.lda + c) * P;
+      double v = fabs(x[0]);
+      for (int l = 1; l < P; ++l) v = v + fabs(x[l]);
+      mx = fmax(mx, v);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) exps[b.offE + r] = scale_exp(mx);
+  } else {
+    __shared__ double red[8][32];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int c = 32 * (lu - b.scale_b_off) + tx;
+    double mx = 0.0;
+    if (c < b.n) {
+      for (int r = ty; r < b.k; r += 8) {
+        const double *x = b.B + ((size_t)r * b.ldb + c) * P;
+        double v = fabs(x[0]);
+        for (int l = 1; l < P; ++l) v = v + fabs(x[l]);
+        mx = fmax(mx, v);
+      }
+    }
+    red[ty][tx] = mx;
+    __syncthreads();
+    if (ty == 0 && c < b.n) {
+#pragma unroll
+      for (int y = 1; y < 8; ++y) mx = fmax(mx, red[y][tx]);
+      exps[b.offF + c] = scale_exp(mx);
+    }
   }
+}
+
+// Digits of one unit: a digit row (row of A's planes or, transposed, column
+// of B's) over 512 k-positions, four per thread.
+template <int NW>
+__device__ __forceinline__ void digits_unit(const BatchProblem &b, const int *exps, int lu) {
+  const int kblocks = (b.Kp + 511) / 512;
+  const bool side_b = lu >= b.dig_b_off;
+  if (side_b) lu -= b.dig_b_off;
+  const int prow = lu / kblocks, pc0 = (lu - prow * kblocks) * 512 + 4 * threadIdx.x;
+  if (!side_b)
+    digits_elem4<NW>(b.p, b.s, b.m, b.k, b.A, b.lda, exps + b.offE, 0, b.dA, b.Kp, b.plane_a,
+                     b.Mp, b.Kp, prow, pc0);
+  else
+    digits_elem4<NW>(b.p, b.s, b.n, b.k, b.B, b.ldb, exps + b.offF, 1, b.dB, b.Kp, b.plane_b,
+                     b.Np, b.Kp, prow, pc0);
+}
+
+template <int NWMAX>
+__global__ void __launch_bounds__(128)
+    digits_all(const BatchProblem *__restrict__ pr, int count, const int *__restrict__ exps) {
+  const int u = blockIdx.x;
+  const BatchProblem &b = pr[find_problem<kDigitUnits>(pr, count, u)];
+  const int lu = u - b.dig_begin;
+  switch (batch_words(b.p)) {
+    case 4: digits_unit<4>(b, exps, lu); break;
+    case 6: if constexpr (NWMAX >= 6) digits_unit<6>(b, exps, lu); break;
+    case 10: if constexpr (NWMAX >= 10) digits_unit<10>(b, exps, lu); break;
+    default: if constexpr (NWMAX >= 16) digits_unit<16>(b, exps, lu); break;
+  }
+}
+
+// Renormalisation of one unit: output row r, 128 V columns.
+template <int P>
+__device__ __forceinline__ void renorm_unit(const BatchProblem &b, const int *exps, int lu) {
+  constexpr int V = batch_cols_per_thread(P);
+  const int nb = (b.n + 128 * V - 1) / (128 * V);
+  const int r = lu / nb, c0 = (lu - r * nb) * 128 * V + V * (int)threadIdx.x;
+  renorm_elems<P, batch_words(P), V>(b.s, b.D, b.Kp / 64, b.m, b.n, b.chunks, b.plane_c, b.Np,
+                                     exps + b.offE, exps + b.offF, b.C, b.ldc, r, c0);
+}
+
+template <int NWMAX>
+__global__ void __launch_bounds__(128)
+    renorm_all(const BatchProblem *__restrict__ pr, int count, const int *__restrict__ exps) {
+  const int u = blockIdx.x;
+  const BatchProblem &b = pr[find_problem<kRenormUnits>(pr, count, u)];
+  const int lu = u - b.out_begin;
+  switch (b.p) {
+    case 2: renorm_unit<2>(b, exps, lu); break;
+    case 4: if constexpr (NWMAX >= 6) renorm_unit<4>(b, exps, lu); break;
+    case 8: if constexpr (NWMAX >= 10) renorm_unit<8>(b, exps, lu); break;
+    default: if constexpr (NWMAX >= 16) renorm_unit<16>(b, exps, lu); break;
+  }
+}
+
+template <int NWMAX>
+int launch_batch_scale(const BatchProblem *pr, int count, int units, int *exps, cudaStream_t st) {
+  if (units == 0) return MDG_SUCCESS;
+  scale_all<NWMAX><<<units, 256, 0, st>>>(pr, count, exps);
+  MDG_TRY_LAUNCH();
+  return MDG_SUCCESS;
+}
+
+template <int NWMAX>
+int launch_batch_digits(const BatchProblem *pr, int count, int units, const int *exps,
+                        cudaStream_t st) {
+  if (units == 0) return MDG_SUCCESS;
+  digits_all<NWMAX><<<units, 128, 0, st>>>(pr, count, exps);
+  MDG_TRY_LAUNCH();
+  return MDG_SUCCESS;
+}
+
+template <int NWMAX>
+int launch_batch_renorm(const BatchProblem *pr, int count, int units, const int *exps,
+                        cudaStream_t st) {
+  if (units == 0) return MDG_SUCCESS;
+  renorm_all<NWMAX><<<units, 128, 0, st>>>(pr, count, exps);
+  MDG_TRY_LAUNCH();
+  return MDG_SUCCESS;
 }
 
 }  // namespace mdgi

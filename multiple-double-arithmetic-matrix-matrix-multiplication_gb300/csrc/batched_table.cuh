@@ -9,47 +9,67 @@
 
 namespace mdgi {
 
+// Integer words of the digit and renormalisation stages for P limbs at the
+// default digit count (words_for(s, 1) and words_for(1, D), s = D).
+__host__ __device__ constexpr int batch_words(int p) {
+  return p == 2 ? 4 : p == 4 ? 6 : p == 8 ? 10 : 16;
+}
+
+// Columns per thread of the renormalisation for P limbs (vector loads of
+// the chunk planes; fewer for the wider integers to bound registers).
+__host__ __device__ constexpr int batch_cols_per_thread(int p) {
+  return p <= 4 ? 4 : p == 8 ? 2 : 1;
+}
+
+// Every stage kernel runs over a flat list of work units (thread blocks);
+// each problem owns a contiguous range of units in every list.
+//   scale:  ceil(m / 8) blocks of 8 rows of A, then ceil(n / 32) blocks of
+//           32 columns of B
+//   digits: Mp x ceil(Kp / 512) blocks of A's digit rows, then
+//           Np x ceil(Kp / 512) of B's
+//   renorm: m x ceil(n / (128 V)) blocks of output rows
 struct BatchProblem {
   int p, s, D, m, n, k, Mp, Np, Kp;
   const double *A, *B;
   double *C;
   int lda, ldb, ldc;
-  int offE, offF;  // row maxima / exponents of A at offE, of B's columns at offF
+  int offE, offF;  // exponents of A's rows at offE, of B's columns at offF
   __nv_bfloat16 *dA, *dB;
   int *chunks;
   long long plane_a, plane_b, plane_c;
-  int rowblk_begin;  // absmax of A: blocks of 256 rows
-  int colblk_begin;  // absmax of B: blocks of 256 rows of B (k)
-  int digA_begin;    // digits of A: rows Mp
-  int digB_begin;    // digits of B: rows Np
-  int out_begin;     // renorm: rows m
+  int scale_begin, scale_b_off;  // first scale unit; units of A's rows
+  int dig_begin, dig_b_off;      // first digit unit; units of A's digit rows
+  int out_begin;                 // first renorm unit
 };
 
-// First problem whose prefix count (Field: 0 row blocks of A, 1 row blocks
-// of B, 2 digit rows of A, 3 digit rows of B, 4 output rows) is <= x.
+enum { kScaleUnits = 0, kDigitUnits = 1, kRenormUnits = 2 };
+
+// The problem whose range of units (Field) holds unit x: the last problem
+// whose first unit is <= x.
 template <int Field>
 __device__ __forceinline__ int find_problem(const BatchProblem *pr, int count, int x) {
   int lo = 0, hi = count - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    const int b = Field == 0 ? pr[mid].rowblk_begin
-                  : Field == 1 ? pr[mid].colblk_begin
-                  : Field == 2 ? pr[mid].digA_begin
-                  : Field == 3 ? pr[mid].digB_begin
-                               : pr[mid].out_begin;
+    const int b = Field == kScaleUnits ? pr[mid].scale_begin
+                  : Field == kDigitUnits ? pr[mid].dig_begin
+                                         : pr[mid].out_begin;
     if (b <= x) lo = mid; else hi = mid - 1;
   }
   return lo;
 }
 
-// Digits of the A and B of one P group (digit-row blocks from xa / xb),
-// and the renormalisation of its C (`rows` output rows from x0), with NW-word
-// integers (instantiated in batched_w{4,6,10,16}.cu).
-template <int NW>
-int launch_batch_digits(const BatchProblem *pr, int count, const int *E, dim3 ga, dim3 gb,
-                        int xa, int xb, cudaStream_t st);
-template <int NW>
-int launch_batch_renorm(int p, const BatchProblem *pr, int count, const int *E, int rows,
-                        int max_n, int x0, cudaStream_t st);
+// One launch each over every problem of the batch: exponents, digits and
+// renormalisation.  NWMAX is the widest integer of the batch (4, 6, 10 or 16
+// words, the P of its widest problem); the kernels switch on each problem's
+// P (instantiated in batched_w{4,6,10,16}.cu).
+template <int NWMAX>
+int launch_batch_scale(const BatchProblem *pr, int count, int units, int *exps, cudaStream_t st);
+template <int NWMAX>
+int launch_batch_digits(const BatchProblem *pr, int count, int units, const int *exps,
+                        cudaStream_t st);
+template <int NWMAX>
+int launch_batch_renorm(const BatchProblem *pr, int count, int units, const int *exps,
+                        cudaStream_t st);
 
 }  // namespace mdgi

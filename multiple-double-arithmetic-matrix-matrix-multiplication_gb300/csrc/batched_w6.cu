@@ -1,8 +1,10 @@
-// Batched digit and renormalisation kernels with 6-word integers
-// (see batched_stages.cuh).
+// Batched exponent, digit and renormalisation kernels for batches whose
+// widest problem needs 6-word integers (see batched_stages.cuh).
 #include "batched_stages.cuh"
 
-template int mdgi::launch_batch_digits<6>(const mdgi::BatchProblem *, int, const int *, dim3,
-                                           dim3, int, int, cudaStream_t);
-template int mdgi::launch_batch_renorm<6>(int, const mdgi::BatchProblem *, int, const int *,
-                                           int, int, int, cudaStream_t);
+template int mdgi::launch_batch_scale<6>(const mdgi::BatchProblem *, int, int, int *,
+                                          cudaStream_t);
+template int mdgi::launch_batch_digits<6>(const mdgi::BatchProblem *, int, int, const int *,
+                                           cudaStream_t);
+template int mdgi::launch_batch_renorm<6>(const mdgi::BatchProblem *, int, int, const int *,
+                                           cudaStream_t);

@@ -132,6 +132,15 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b
       "l"(a), "l"(b), "r"(IDESC), "r"(acc));
 }
 
+// The same with a run-time instruction descriptor (tile width per job).
+__device__ __forceinline__ void mma_bf16_n(uint32_t d_tmem, uint64_t a, uint64_t b,
+                                           uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
@@ -180,6 +189,17 @@ __device__ __forceinline__ void add_exact(int *acc, const uint32_t (&r)[32]) {
   for (int j = 0; j < 32; ++j) acc[j] += __float2int_rn(__uint_as_float(r[j]));
 }
 
+// Adds 64 accumulator columns (starting at taddr) into acc[0..63].
+__device__ __forceinline__ void drain64(uint32_t taddr, int (&acc)[128]) {
+  uint32_t ra[32], rb[32];
+  tmem_ld32(taddr, ra);
+  tmem_wait(ra);
+  tmem_ld32(taddr + 32, rb);
+  add_exact(acc, ra);
+  tmem_wait(rb);
+  add_exact(acc + 32, rb);
+}
+
 // Adds 128 accumulator columns (starting at taddr) into acc: four 32-column
 // loads, each issued before the previous block is converted so that the
 // load latency overlaps the integer work.
@@ -200,10 +220,12 @@ __device__ __forceinline__ void drain128(uint32_t taddr, int (&acc)[128]) {
 }
 
 // One tile of work: where its operands and output live and which of its
-// problem's rows / columns it covers.
+// problem's rows / columns it covers.  tn: tile width, 256 or 128 columns
+// (the B box of tmB is tn rows); ktail: MMAs of K = 16 issued for the last
+// k-block (1..4; the rest of that block is the zero padding of k).
 struct TileJob {
   const CUtensorMap *tmA, *tmB;
-  int s, D, Mp, Np, KB, row, col;
+  int s, D, Mp, Np, KB, row, col, tn, ktail;
   int *out;
   long long plane_c;
 };
@@ -217,7 +239,8 @@ struct SingleJobs {
   __device__ int tiles() const { return (Mp / TM) * (Np / TN); }
   __device__ TileJob job(int t) const {
     const int MB = Mp / TM;
-    return TileJob{tmA, tmB, s, D, Mp, Np, KB, (t % MB) * TM, (t / MB) * TN, out, plane_c};
+    return TileJob{tmA, tmB, s, D, Mp, Np, KB, (t % MB) * TM, (t / MB) * TN, TN, TK / 16,
+                   out, plane_c};
   }
 };
 
@@ -283,7 +306,7 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
           for (int t = 0; t < S; ++t) {
             const int i = ilo + t / KB, kb = t - (t / KB) * KB, j = d - i;
             if (!mbar_wait(empty(st), ph ^ 1, abort_flag)) goto producer_done;
-            mbar_expect_tx(full(st), STAGE_BYTES);
+            mbar_expect_tx(full(st), A_BYTES + jb.tn * TK * 2);
             const uint32_t a_dst = smem_base + st * STAGE_BYTES;
             tma_load_2d(a_dst, jb.tmA, kb * TK, i * jb.Mp + jb.row, full(st));
             tma_load_2d(a_dst + A_BYTES, jb.tmB, kb * TK, j * jb.Np + jb.col, full(st));
@@ -309,6 +332,7 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
       bool any = false;
       for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const TileJob jb = jobs.job(tile);
+        const uint32_t idesc = (IDESC & ~(0x3Fu << 17)) | ((uint32_t)(jb.tn >> 3) << 17);
         for (int d = 0; d < jb.D; ++d) {
           const int S = mdgi::diag_pairs(d, jb.s) * jb.KB;
           for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
@@ -321,9 +345,12 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
               fence_after();
               const uint32_t a_addr = smem_base + st * STAGE_BYTES;
               const uint64_t da = sw128_desc(a_addr), db = sw128_desc(a_addr + A_BYTES);
+              // the last k-block of a pair: only the MMAs that reach data
+              const int nsub = (t % jb.KB == jb.KB - 1) ? jb.ktail : TK / 16;
 #pragma unroll
               for (int kk = 0; kk < TK / 16; ++kk)
-                mma_bf16(dt, da + 2 * kk, db + 2 * kk, (t > g0 || kk > 0) ? 1u : 0u);
+                if (kk < nsub)
+                  mma_bf16_n(dt, da + 2 * kk, db + 2 * kk, idesc, (t > g0 || kk > 0) ? 1u : 0u);
               mma_commit(empty(st));
               any = true;
               if (++st == STAGES) {
@@ -353,8 +380,9 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
     uint32_t aph[2] = {0, 0};
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
       const TileJob jb = jobs.job(tile);
+      const bool wide = jb.tn == TN;  // 128 columns per warp, else 64
       const int row = jb.row + 32 * q + lane;
-      const int col = jb.col + 128 * h;
+      const int col = jb.col + (wide ? 128 : 64) * h;
       int chunk = 0;
       for (int d = 0; d < jb.D; ++d) {
         const int S = mdgi::diag_pairs(d, jb.s) * jb.KB;
@@ -367,8 +395,12 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
           if (!ok) goto epi_done;
           aph[buf] ^= 1;
           fence_after();
-          const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + buf * TN + 128 * h;
-          drain128(taddr, acc);
+          const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + buf * TN +
+                                 (wide ? 128 : 64) * h;
+          if (wide)
+            drain128(taddr, acc);
+          else
+            drain64(taddr, acc);
           fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(accempty(buf));
@@ -377,10 +409,18 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
           if (g1 % mdgi::CHUNK_STEPS == 0 || g1 >= S) {
             int4 *dst = reinterpret_cast<int4 *>(jb.out + (size_t)chunk * jb.plane_c +
                                                  (size_t)row * jb.Np + col);
+            if (wide) {
 #pragma unroll
-            for (int v = 0; v < 32; ++v) {
-              dst[v] = make_int4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
-              acc[4 * v] = acc[4 * v + 1] = acc[4 * v + 2] = acc[4 * v + 3] = 0;
+              for (int v = 0; v < 32; ++v) {
+                dst[v] = make_int4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
+                acc[4 * v] = acc[4 * v + 1] = acc[4 * v + 2] = acc[4 * v + 3] = 0;
+              }
+            } else {
+#pragma unroll
+              for (int v = 0; v < 16; ++v) {
+                dst[v] = make_int4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
+                acc[4 * v] = acc[4 * v + 1] = acc[4 * v + 2] = acc[4 * v + 3] = 0;
+              }
             }
             ++chunk;
           }
@@ -423,8 +463,8 @@ struct GroupedJobs {
     const mdgi::GroupedProblem &g = probs[lo];
     const int lt = t - g.tile_begin, MB = g.Mp / TM;
     return TileJob{reinterpret_cast<const CUtensorMap *>(g.tmA),
-                   reinterpret_cast<const CUtensorMap *>(g.tmB), g.s, g.D, g.Mp, g.Np, g.KB, (lt % MB) * TM, (lt / MB) * TN,
-                   g.out, g.plane_c};
+                   reinterpret_cast<const CUtensorMap *>(g.tmB), g.s, g.D, g.Mp, g.Np, g.KB,
+                   (lt % MB) * TM, (lt / MB) * g.tn, g.tn, g.ktail, g.out, g.plane_c};
   }
 };
 

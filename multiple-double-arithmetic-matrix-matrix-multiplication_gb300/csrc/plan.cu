@@ -9,7 +9,9 @@
 // name>|<driver version>") and shape class ("<form> <P> <s> <D> <Mp> <Np>
 // <Kp>", the padded sizes the kernels see); mdg_tune_cache_save / _load keep
 // it as a small JSON file.  Slice and diagonal counts change the rounding, so
-// they stay the caller's options and are part of the key, not tuned.
+// they stay the caller's options and are part of the key, not tuned.  The
+// batched plan (batched.cu) records its tile policy here too, under "batch
+// <count> <hash of the problem shapes>".
 #include <cctype>
 #include <cstdio>
 #include <cstdlib>
@@ -22,8 +24,10 @@
 
 namespace {
 
+// A single-problem schedule (engine, parts, raster), or for a batched plan
+// ("batch ..." keys) its tile policy.
 struct TuneEntry {
-  int engine = 0, parts = 0, raster = 0;
+  int engine = 0, parts = 0, raster = 0, tiles = 0;
   double ms = 0.0;
 };
 
@@ -117,6 +121,29 @@ std::string quoted(const std::string &s) {
 }
 
 }  // namespace
+
+namespace mdgi {
+
+void tune_lookup_batch(const std::string &key, int *policy) {
+  std::string dev;
+  if (device_key(&dev) != MDG_SUCCESS) return;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto d = g_tune.find(dev);
+  if (d == g_tune.end()) return;
+  auto e = d->second.find(key);
+  if (e != d->second.end()) *policy = e->second.tiles;
+}
+
+void tune_record_batch(const std::string &key, int policy, double ms) {
+  std::string dev;
+  if (device_key(&dev) != MDG_SUCCESS) return;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  TuneEntry &t = g_tune[dev][key];
+  t.tiles = policy;
+  t.ms = ms;
+}
+
+}  // namespace mdgi
 
 struct mdg_plan_s {
   int form, p, m, n, k;
@@ -276,6 +303,7 @@ int mdg_tune_cache_load(const char *path) {
         if (field == "engine") return whole_in(v, 0, 3, &e.engine);
         if (field == "parts") return whole_in(v, 0, 8, &e.parts);
         if (field == "raster") return whole_in(v, 0, 1 << 20, &e.raster);
+        if (field == "tiles") return whole_in(v, 0, 2, &e.tiles);
         if (field == "ms") {
           if (!(v >= 0.0 && v <= 1e12)) return false;
           e.ms = v;
@@ -306,9 +334,13 @@ int mdg_tune_cache_save(const char *path) {
       bool first = true;
       for (auto &e : d.second) {
         char buf[160];
-        std::snprintf(buf, sizeof(buf),
-                      "{\"engine\": %d, \"parts\": %d, \"raster\": %d, \"ms\": %.4f}",
-                      e.second.engine, e.second.parts, e.second.raster, e.second.ms);
+        if (e.first.compare(0, 6, "batch ") == 0)
+          std::snprintf(buf, sizeof(buf), "{\"tiles\": %d, \"ms\": %.4f}", e.second.tiles,
+                        e.second.ms);
+        else
+          std::snprintf(buf, sizeof(buf),
+                        "{\"engine\": %d, \"parts\": %d, \"raster\": %d, \"ms\": %.4f}",
+                        e.second.engine, e.second.parts, e.second.raster, e.second.ms);
         out += (first ? "\n    " : ",\n    ") + quoted(e.first) + ": " + buf;
         first = false;
       }

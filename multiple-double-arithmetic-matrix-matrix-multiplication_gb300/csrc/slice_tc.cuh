@@ -1,6 +1,8 @@
 // Internal interface of the slice-digit form (slice_tc.cu, diag_gemm_tc.cu).
 #pragma once
 
+#include <string>
+
 #include <cuda_runtime.h>
 #include <stddef.h>
 
@@ -70,16 +72,23 @@ int launch_renorm(int p, int s, int D, int KB, int m, int n, const int *chunks,
                   long long plane_c, int ldcd, const int *E, const int *F, double *C, int ldc,
                   cudaStream_t st);
 // One problem of a grouped diagonal GEMM (single-CTA tcgen05 kernel,
-// 128 x 256 tiles): tensor maps of its digit planes, sizes, first global
-// tile, output chunk planes.  Lives in global memory, 64-byte aligned.
+// tiles of 128 rows x tn columns, tn = 256 or 128): tensor maps of its digit
+// planes, sizes, first global tile, column tiles nt, output chunk planes.
+// ktail: MMAs of K = 16 that reach data in the last 64-deep k-block (1..4).
+// Lives in global memory, 64-byte aligned.
 struct alignas(64) GroupedProblem {
   unsigned char tmA[128];  // CUtensorMap, A planes, box 64 x 128
-  unsigned char tmB[128];  // CUtensorMap, B planes, box 64 x 256
-  int s, D, Mp, Np, KB, tile_begin;
+  unsigned char tmB[128];  // CUtensorMap, B planes, box 64 x tn
+  int s, D, Mp, Np, KB, tile_begin, tn, nt, ktail;
   int *out;
   long long plane_c;
 };
 int encode_plane_map(void *map128, const void *base, int Kp, long long rows_total, int box_rows);
+// The batched plan's entries in the tuning cache (plan.cu), under the
+// current device: the tile policy recorded for a batch key, if any
+// (*policy is left alone otherwise), and a new record.
+void tune_lookup_batch(const std::string &key, int *policy);
+void tune_record_batch(const std::string &key, int policy, double ms);
 int launch_diag_gemm_grouped(const GroupedProblem *dev_probs, int count, int total_tiles,
                              cudaStream_t st);
 
