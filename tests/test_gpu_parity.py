@@ -514,3 +514,45 @@ def test_batched_plan_graph_capture(api, orc, inputs):
     for (P, m, n, k), (A, B), C in list(zip(probs, ops, plan.Cs))[:3]:
         sl = api.default_slices(P)
         assert np.array_equal(host(C), orc.gemm_slices(P, sl, sl, A, B, m, n, k))
+
+
+def test_batched_tile_policies_bit_identical_and_tuned(api, orc, inputs):
+    """The grouped GEMM under each tile policy (256-column tiles, 128-column
+    tiles, and the per-problem choice) over problems whose n falls on both
+    sides of a 256 boundary and whose k ends inside a 64-deep block (the
+    last block issues fewer MMAs): every problem's C equals the
+    single-problem GEMM under every policy; tuning keeps one of them and
+    records it for plans of the same shapes."""
+    rng = np.random.default_rng(31)
+    probs = [(2, 96, 300, 40), (4, 130, 100, 96), (8, 64, 384, 160), (2, 256, 512, 16),
+             (4, 33, 129, 200), (16, 20, 140, 24), (8, 128, 250, 64)]
+    ops = [(dev(inputs.uniform_pd(rng, (m, k), P)), dev(inputs.uniform_pd(rng, (k, n), P)))
+           for P, m, n, k in probs]
+    want = [api.gemm(A, B, "slice_bf16") for A, B in ops]
+    plan = api.BatchPlan(ops)
+    assert plan.tiles == "auto"
+    for policy in ("256", "128", "auto"):
+        plan.set_tiles(policy)
+        for C in plan.Cs:
+            C.fill_(np.nan)
+        plan.run()
+        torch.cuda.synchronize()
+        for i, (C, W) in enumerate(zip(plan.Cs, want)):
+            assert torch.equal(C, W), (policy, probs[i])
+    api.tune_cache_clear()
+    best = plan.tune()
+    assert best in ("auto", "256", "128")
+    assert api.tune_cache_size() == 1
+    again = api.BatchPlan(ops)  # same shapes: starts with the tuned policy
+    assert again.tiles == best
+    again.run()
+    torch.cuda.synchronize()
+    for C, W in zip(again.Cs, want):
+        assert torch.equal(C, W)
+    api.tune_cache_clear()
+    # the first problem against the oracle as well
+    P, m, n, k = probs[0]
+    s = api.default_slices(P)
+    A, B = host(ops[0][0]), host(ops[0][1])
+    assert np.array_equal(host(again.Cs[0]), orc.gemm_slices(P, s, s, A, B, m, n, k))
+    assert api.device_status() == 0
