@@ -145,7 +145,7 @@ int plan_batch(const mdg_problem *problems, int count, Layout *L, mdg_batch_s *h
     const int nw = std::max(mdgi::words_for(s, 1), mdgi::words_for(1, D));
     if (!nw || nw > mdgi::batch_words(q.p)) return MDG_ERROR_NOT_SUPPORTED;
     h->nwmax = std::max(h->nwmax, mdgi::batch_words(q.p));
-    const int kblocks = (Kp + 511) / 512;
+    const int kblocks = (Kp + 127) / 128;
     const int V = mdgi::batch_cols_per_thread(q.p);
     const int scale_a = (q.m + 7) / 8, scale_b = (q.n + 31) / 32;
     const int digit_a = Mp * kblocks, digit_b = Np * kblocks;

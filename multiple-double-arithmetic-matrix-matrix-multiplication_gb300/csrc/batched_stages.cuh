@@ -64,19 +64,21 @@ __global__ void __launch_bounds__(256)
 }
 
 // Digits of one unit: a digit row (row of A's planes or, transposed, column
-// of B's) over 512 k-positions, four per thread.
+// of B's) over 128 k-positions, one per thread (one element per thread
+// keeps the wide integers of the octo- and hexa-double branches few, so
+// the merged kernel's register count stays near the single-width ones').
 template <int NW>
 __device__ __forceinline__ void digits_unit(const BatchProblem &b, const int *exps, int lu) {
-  const int kblocks = (b.Kp + 511) / 512;
+  const int kblocks = (b.Kp + 127) / 128;
   const bool side_b = lu >= b.dig_b_off;
   if (side_b) lu -= b.dig_b_off;
-  const int prow = lu / kblocks, pc0 = (lu - prow * kblocks) * 512 + 4 * threadIdx.x;
+  const int prow = lu / kblocks, pc = (lu - prow * kblocks) * 128 + (int)threadIdx.x;
   if (!side_b)
-    digits_elem4<NW>(b.p, b.s, b.m, b.k, b.A, b.lda, exps + b.offE, 0, b.dA, b.Kp, b.plane_a,
-                     b.Mp, b.Kp, prow, pc0);
+    digits_elem<NW>(b.p, b.s, b.m, b.k, b.A, b.lda, exps + b.offE, 0, b.dA, b.Kp, b.plane_a,
+                    b.Mp, b.Kp, prow, pc);
   else
-    digits_elem4<NW>(b.p, b.s, b.n, b.k, b.B, b.ldb, exps + b.offF, 1, b.dB, b.Kp, b.plane_b,
-                     b.Np, b.Kp, prow, pc0);
+    digits_elem<NW>(b.p, b.s, b.n, b.k, b.B, b.ldb, exps + b.offF, 1, b.dB, b.Kp, b.plane_b,
+                    b.Np, b.Kp, prow, pc);
 }
 
 template <int NWMAX>

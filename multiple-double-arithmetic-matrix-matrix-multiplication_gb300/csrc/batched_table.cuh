@@ -25,8 +25,8 @@ __host__ __device__ constexpr int batch_cols_per_thread(int p) {
 // each problem owns a contiguous range of units in every list.
 //   scale:  ceil(m / 8) blocks of 8 rows of A, then ceil(n / 32) blocks of
 //           32 columns of B
-//   digits: Mp x ceil(Kp / 512) blocks of A's digit rows, then
-//           Np x ceil(Kp / 512) of B's
+//   digits: Mp x ceil(Kp / 128) blocks of A's digit rows, then
+//           Np x ceil(Kp / 128) of B's
 //   renorm: m x ceil(n / (128 V)) blocks of output rows
 struct BatchProblem {
   int p, s, D, m, n, k, Mp, Np, Kp;

@@ -335,6 +335,7 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
         const uint32_t idesc = (IDESC & ~(0x3Fu << 17)) | ((uint32_t)(jb.tn >> 3) << 17);
         for (int d = 0; d < jb.D; ++d) {
           const int S = mdgi::diag_pairs(d, jb.s) * jb.KB;
+          int kb = 0;  // k-block of step t within its digit pair
           for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
             if (!mbar_wait(accempty(buf), aph[buf] ^ 1, abort_flag)) goto mma_done;
             fence_after();
@@ -346,7 +347,8 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
               const uint32_t a_addr = smem_base + st * STAGE_BYTES;
               const uint64_t da = sw128_desc(a_addr), db = sw128_desc(a_addr + A_BYTES);
               // the last k-block of a pair: only the MMAs that reach data
-              const int nsub = (t % jb.KB == jb.KB - 1) ? jb.ktail : TK / 16;
+              const int nsub = (kb == jb.KB - 1) ? jb.ktail : TK / 16;
+              if (++kb == jb.KB) kb = 0;
 #pragma unroll
               for (int kk = 0; kk < TK / 16; ++kk)
                 if (kk < nsub)

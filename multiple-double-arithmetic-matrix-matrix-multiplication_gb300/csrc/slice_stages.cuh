@@ -123,26 +123,13 @@ __device__ __forceinline__ void digits_elem4(int P, int s, int rows, int cols,
 #pragma unroll
     for (int i = 0; i < NW; ++i) w[e][i] = 0;
   }
-  // limb l of the four entries is loaded while limb l - 1 is being added,
-  // so eight loads are in flight rather than one
-  const double *a[4];
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
-    const int pc = pc0 + e < cols ? pc0 + e : cols - 1;  // past the end: a valid address
-    a[e] = trans ? X + ((size_t)pc * ldx + pr) * P : X + ((size_t)pr * ldx + pc) * P;
-  }
-  double cur[4], nxt[4];
-#pragma unroll
-  for (int e = 0; e < 4; ++e) cur[e] = a[e][0];
-  for (int l = 0; l < P; ++l) {
-    if (l + 1 < P) {
-#pragma unroll
-      for (int e = 0; e < 4; ++e) nxt[e] = a[e][l + 1];
-    }
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
+    const int pc = pc0 + e;
+    const double *a = trans ? X + ((size_t)pc * ldx + pr) * P : X + ((size_t)pr * ldx + pc) * P;
+    for (int l = 0; l < P; ++l) {
       int e2;
-      const int64_t m = pc0 + e < cols ? mdgi::exact_significand(cur[e], e2) : 0;
+      const int64_t m = pc < cols ? mdgi::exact_significand(a[l], e2) : 0;
       if (m == 0) continue;
       const int q = e2 + S - Er;
       if (q >= 0) {
@@ -153,8 +140,6 @@ __device__ __forceinline__ void digits_elem4(int P, int s, int rows, int cols,
         mdgi::wide_add_shifted<NW>(w[e], m < 0 ? -1 : 0, 0);
       }
     }
-#pragma unroll
-    for (int e = 0; e < 4; ++e) cur[e] = nxt[e];
   }
   int carry[4] = {0, 0, 0, 0};
 #pragma unroll
@@ -193,10 +178,7 @@ __device__ __forceinline__ void digits_elem4(int P, int s, int rows, int cols,
 // diagonal 0, T is the top part of W, above bit 8 (D - 1).  The emitted
 // bytes land at positions fixed at compile time, so W stays in registers.
 // Each thread takes V adjacent columns and loads their chunk sums as one
-// vector per chunk plane.  The loads of RG diagonals (their first RNC
-// chunks each) are issued together before any of them is added, so a
-// thread has up to RG * RNC loads in flight instead of one: the sums are
-// consumed in order, but the memory latency is paid once per group.
+// vector per chunk plane.
 template <int V>
 struct IntV;
 template <>
@@ -218,15 +200,12 @@ struct IntV<1> {
   static __device__ __forceinline__ void load(const int *p, int (&x)[1]) { x[0] = *p; }
 };
 
-constexpr int RG = 8;  // diagonals whose loads are issued together
-
 template <int P, int NW, int V>
 __device__ __forceinline__ void renorm_elems(int s, int D, int KB, int m, int n,
                                              const int *__restrict__ chunks, long long plane_c,
                                              int ldcd, const int *__restrict__ E,
                                              const int *__restrict__ F, double *__restrict__ C,
                                              int ldc, int r, int c0) {
-  constexpr int RNC = V == 4 ? 1 : 2;  // chunks per diagonal loaded up front
   if (c0 >= n || r >= m) return;
   const int *src = chunks + (size_t)r * ldcd + c0;
   int q = 0;
@@ -240,52 +219,25 @@ __device__ __forceinline__ void renorm_elems(int s, int D, int KB, int m, int n,
     for (int i = 0; i < NW; ++i) w[v][i] = 0;
   }
 #pragma unroll
-  for (int k0 = 0; k0 < 8 * NW; k0 += RG) {
-    if (k0 < D) {
-      // issue the loads of diagonals D-1-k0 .. D-RG-k0 (chunk indices fall)
-      int x[RG][RNC][V], qs[RG], ncs[RG];
+  for (int wi = 0; wi < NW; ++wi) {
 #pragma unroll
-      for (int g = 0; g < RG; ++g) {
-        const int k = k0 + g;
-        ncs[g] = 0;
-        qs[g] = q;
-        if (k < D) {
-          ncs[g] = mdgi::diag_chunks(D - 1 - k, s, KB);
-          q -= ncs[g];
-          qs[g] = q;
+    for (int b = 0; b < 8; ++b) {
+      const int k = wi * 8 + b;
+      if (k < D) {
+        const int d = D - 1 - k;
+        const int nc = mdgi::diag_chunks(d, s, KB);
+        q -= nc;
+        for (int j = 0; j < nc; ++j) {
+          int x[V];
+          IntV<V>::load(src + (size_t)(q + j) * plane_c, x);
+#pragma unroll
+          for (int v = 0; v < V; ++v) T[v] += x[v];
         }
+        if (k < D - 1) {
 #pragma unroll
-        for (int j = 0; j < RNC; ++j) {
-          if (j < ncs[g]) {
-            IntV<V>::load(src + (size_t)(qs[g] + j) * plane_c, x[g][j]);
-          } else {
-#pragma unroll
-            for (int v = 0; v < V; ++v) x[g][j][v] = 0;
-          }
-        }
-      }
-      // then add them in order, one emitted byte per diagonal
-#pragma unroll
-      for (int g = 0; g < RG; ++g) {
-        const int k = k0 + g;
-        if (k < D) {
-#pragma unroll
-          for (int j = 0; j < RNC; ++j) {
-#pragma unroll
-            for (int v = 0; v < V; ++v) T[v] += x[g][j][v];
-          }
-          for (int j = RNC; j < ncs[g]; ++j) {  // diagonals of more chunks
-            int y[V];
-            IntV<V>::load(src + (size_t)(qs[g] + j) * plane_c, y);
-#pragma unroll
-            for (int v = 0; v < V; ++v) T[v] += y[v];
-          }
-          if (k < D - 1) {
-#pragma unroll
-            for (int v = 0; v < V; ++v) {
-              w[v][k / 8] |= (uint64_t)(T[v] & 255) << (8 * (k % 8));
-              T[v] >>= 8;
-            }
+          for (int v = 0; v < V; ++v) {
+            w[v][wi] |= (uint64_t)(T[v] & 255) << (8 * b);
+            T[v] >>= 8;
           }
         }
       }
