@@ -142,12 +142,12 @@ void mdg_release_cache(void);
  * out `workspace` (mdg_batch_workspace_size bytes) for these problems
  * (device pointers, P in {2,4,8,16}, m, n, k >= 1, default digits per P),
  * uploads the per-problem tables and tensor maps and returns a handle;
- * it synchronises `stream`.  mdg_batch_run only launches kernels (4 per
- * batch, whatever the mix of P: exponents of every row and column, digits
- * of every operand, one grouped tcgen05 diagonal GEMM over the tiles of
- * every problem, renormalisation of every C) and may be captured into a
- * CUDA graph; each C equals the single-problem mdg_gemm result bit for bit.
- * No counterpart in the reference. */
+ * it synchronises `stream`.  mdg_batch_run only launches kernels (one for
+ * the exponents of every row and column, one for the digits of every
+ * operand, one grouped tcgen05 diagonal GEMM over the tiles of every
+ * problem, and one renormalisation per limb count present) and may be
+ * captured into a CUDA graph; each C equals the single-problem mdg_gemm
+ * result bit for bit.  No counterpart in the reference. */
 typedef struct mdg_batch_s *mdg_batch;
 size_t mdg_batch_workspace_size(const mdg_problem *problems, int count);
 int mdg_batch_create(const mdg_problem *problems, int count, void *workspace,

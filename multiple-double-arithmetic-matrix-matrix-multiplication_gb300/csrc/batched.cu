@@ -5,11 +5,11 @@
 // the scale exponents of all problems side by side, every problem's digit
 // and chunk planes) and uploads the tables, tensor maps included;
 // mdg_batch_run only launches kernels, so it can be captured into a CUDA
-// graph and replayed.  Four launches per run, whatever the mix of P:
-//   exponents of every row of every A and every column of every B
-//   digits of every A and every B
-//   one grouped tcgen05 diagonal GEMM over the tiles of all problems
-//   renormalisation of every C
+// graph and replayed.  Per run, whatever the mix of P:
+//   one launch: exponents of every row of every A and column of every B
+//   one launch: digits of every A and every B
+//   one launch: grouped tcgen05 diagonal GEMM over the tiles of all problems
+//   one launch per limb count present: renormalisation of its C
 // Each stage kernel finds its problem from its block index by binary search
 // over per-problem prefix counts, and branches on the problem's P to the
 // integer width that P needs (batched_stages.cuh).  The grouped GEMM's tiles
@@ -32,6 +32,7 @@
 struct mdg_batch_s {
   int count = 0, nwmax = 4, total_tiles = 0;
   int scale_units = 0, digit_units = 0, renorm_units = 0;
+  int renorm_begin[4] = {0, 0, 0, 0}, renorm_count[4] = {0, 0, 0, 0};  // per P = 2, 4, 8, 16
   int tiles_policy = MDG_BATCH_TILES_AUTO;
   mdgi::BatchProblem *dprobs = nullptr;
   mdgi::GroupedProblem *dgroups = nullptr;
@@ -125,6 +126,7 @@ int plan_batch(const mdg_problem *problems, int count, Layout *L, mdg_batch_s *h
   L->off_chunks.resize(count);
   int scale_u = 0, digit_u = 0, renorm_u = 0, offE = 0, offF = rows;
   h->nwmax = 4;
+  for (int i = 0; i < 4; ++i) h->renorm_begin[i] = h->renorm_count[i] = 0;
   // the table is kept in order of P (stable): blocks of one P sit together
   // in every stage's launch
   std::vector<int> order(count);
@@ -167,6 +169,9 @@ int plan_batch(const mdg_problem *problems, int count, Layout *L, mdg_batch_s *h
       b.out_begin = renorm_u;
       hp->push_back(b);
     }
+    const int pi = q.p == 2 ? 0 : q.p == 4 ? 1 : q.p == 8 ? 2 : 3;
+    if (h->renorm_count[pi] == 0) h->renorm_begin[pi] = renorm_u;
+    h->renorm_count[pi] += out_u;
     scale_u += scale_a + scale_b;
     digit_u += digit_a + digit_b;
     renorm_u += out_u;
@@ -284,11 +289,9 @@ int mdg_batch_create(const mdg_problem *problems, int count, void *workspace,
 int mdg_batch_run(mdg_batch_s *h, void *stream) {
   if (!h) return MDG_ERROR_NULL_POINTER;
   cudaStream_t st = mdgi::as_stream(stream);
-#define MDG_BATCH_STAGES(W)                                                                \
-  MDG_TRY(mdgi::launch_batch_scale<W>(h->dprobs, h->count, h->scale_units, h->exps, st));  \
-  MDG_TRY(mdgi::launch_batch_digits<W>(h->dprobs, h->count, h->digit_units, h->exps, st)); \
-  MDG_TRY(mdgi::launch_diag_gemm_grouped(h->dgroups, h->count, h->total_tiles, st));       \
-  MDG_TRY(mdgi::launch_batch_renorm<W>(h->dprobs, h->count, h->renorm_units, h->exps, st))
+#define MDG_BATCH_STAGES(W)                                                               \
+  MDG_TRY(mdgi::launch_batch_scale<W>(h->dprobs, h->count, h->scale_units, h->exps, st)); \
+  MDG_TRY(mdgi::launch_batch_digits<W>(h->dprobs, h->count, h->digit_units, h->exps, st))
   switch (h->nwmax) {
     case 4: MDG_BATCH_STAGES(4); break;
     case 6: MDG_BATCH_STAGES(6); break;
@@ -296,6 +299,12 @@ int mdg_batch_run(mdg_batch_s *h, void *stream) {
     default: MDG_BATCH_STAGES(16); break;
   }
 #undef MDG_BATCH_STAGES
+  MDG_TRY(mdgi::launch_diag_gemm_grouped(h->dgroups, h->count, h->total_tiles, st));
+  const int *rb = h->renorm_begin, *rc = h->renorm_count;
+  MDG_TRY(mdgi::launch_batch_renorm<2>(h->dprobs, h->count, rb[0], rc[0], h->exps, st));
+  MDG_TRY(mdgi::launch_batch_renorm<4>(h->dprobs, h->count, rb[1], rc[1], h->exps, st));
+  MDG_TRY(mdgi::launch_batch_renorm<8>(h->dprobs, h->count, rb[2], rc[2], h->exps, st));
+  MDG_TRY(mdgi::launch_batch_renorm<16>(h->dprobs, h->count, rb[3], rc[3], h->exps, st));
   return MDG_SUCCESS;
 }
 

@@ -1,11 +1,12 @@
 // Exponent, digit and renormalisation kernels of the batched slice-digit
-// GEMM: one launch per stage over every problem of the batch, whatever its
-// P.  Each block finds its problem in the table (batched_table.cuh) and
-// branches on the problem's P to the integer width that P needs; the
-// branches of wider integers than the batch holds are not compiled into
-// the instance that is launched (NWMAX).  One translation unit per NWMAX
-// (batched_w{4,6,10,16}.cu) so that the wide-integer code compiles in
-// parallel.
+// GEMM.  The exponent and digit kernels run once over every problem of the
+// batch, whatever its P: each block finds its problem in the table
+// (batched_table.cuh) and branches on the problem's P to the integer width
+// that P needs; the branches of wider integers than the batch holds are not
+// compiled into the instance that is launched (NWMAX).  The
+// renormalisation runs once per limb count present.  One translation unit
+// per width (batched_w{4,6,10,16}.cu) so that the wide-integer code
+// compiles in parallel.
 #pragma once
 
 #include "batched_table.cuh"
@@ -105,18 +106,15 @@ __device__ __forceinline__ void renorm_unit(const BatchProblem &b, const int *ex
                                      exps + b.offE, exps + b.offF, b.C, b.ldc, r, c0);
 }
 
-template <int NWMAX>
+// The renormalisation runs one launch per P: a kernel with the bodies of
+// several widths measured 15 % slower than these (one body each).
+template <int P>
 __global__ void __launch_bounds__(128)
-    renorm_all(const BatchProblem *__restrict__ pr, int count, const int *__restrict__ exps) {
-  const int u = blockIdx.x;
+    renorm_p(const BatchProblem *__restrict__ pr, int count, const int *__restrict__ exps,
+             int unit0) {
+  const int u = unit0 + (int)blockIdx.x;
   const BatchProblem &b = pr[find_problem<kRenormUnits>(pr, count, u)];
-  const int lu = u - b.out_begin;
-  switch (b.p) {
-    case 2: renorm_unit<2>(b, exps, lu); break;
-    case 4: if constexpr (NWMAX >= 6) renorm_unit<4>(b, exps, lu); break;
-    case 8: if constexpr (NWMAX >= 10) renorm_unit<8>(b, exps, lu); break;
-    default: if constexpr (NWMAX >= 16) renorm_unit<16>(b, exps, lu); break;
-  }
+  renorm_unit<P>(b, exps, u - b.out_begin);
 }
 
 template <int NWMAX>
@@ -136,11 +134,11 @@ int launch_batch_digits(const BatchProblem *pr, int count, int units, const int 
   return MDG_SUCCESS;
 }
 
-template <int NWMAX>
-int launch_batch_renorm(const BatchProblem *pr, int count, int units, const int *exps,
+template <int P>
+int launch_batch_renorm(const BatchProblem *pr, int count, int unit0, int units, const int *exps,
                         cudaStream_t st) {
   if (units == 0) return MDG_SUCCESS;
-  renorm_all<NWMAX><<<units, 128, 0, st>>>(pr, count, exps);
+  renorm_p<P><<<units, 128, 0, st>>>(pr, count, exps, unit0);
   MDG_TRY_LAUNCH();
   return MDG_SUCCESS;
 }

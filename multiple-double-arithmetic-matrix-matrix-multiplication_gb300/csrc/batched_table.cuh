@@ -59,17 +59,18 @@ __device__ __forceinline__ int find_problem(const BatchProblem *pr, int count, i
   return lo;
 }
 
-// One launch each over every problem of the batch: exponents, digits and
-// renormalisation.  NWMAX is the widest integer of the batch (4, 6, 10 or 16
+// One launch each over every problem of the batch for the exponents and
+// the digits: NWMAX is the widest integer of the batch (4, 6, 10 or 16
 // words, the P of its widest problem); the kernels switch on each problem's
-// P (instantiated in batched_w{4,6,10,16}.cu).
+// P.  The renormalisation: one launch per P over that P's units
+// [unit0, unit0 + units).  (Instantiated in batched_w{4,6,10,16}.cu.)
 template <int NWMAX>
 int launch_batch_scale(const BatchProblem *pr, int count, int units, int *exps, cudaStream_t st);
 template <int NWMAX>
 int launch_batch_digits(const BatchProblem *pr, int count, int units, const int *exps,
                         cudaStream_t st);
-template <int NWMAX>
-int launch_batch_renorm(const BatchProblem *pr, int count, int units, const int *exps,
+template <int P>
+int launch_batch_renorm(const BatchProblem *pr, int count, int unit0, int units, const int *exps,
                         cudaStream_t st);
 
 }  // namespace mdgi

@@ -189,17 +189,6 @@ __device__ __forceinline__ void add_exact(int *acc, const uint32_t (&r)[32]) {
   for (int j = 0; j < 32; ++j) acc[j] += __float2int_rn(__uint_as_float(r[j]));
 }
 
-// Adds 64 accumulator columns (starting at taddr) into acc[0..63].
-__device__ __forceinline__ void drain64(uint32_t taddr, int (&acc)[128]) {
-  uint32_t ra[32], rb[32];
-  tmem_ld32(taddr, ra);
-  tmem_wait(ra);
-  tmem_ld32(taddr + 32, rb);
-  add_exact(acc, ra);
-  tmem_wait(rb);
-  add_exact(acc + 32, rb);
-}
-
 // Adds 128 accumulator columns (starting at taddr) into acc: four 32-column
 // loads, each issued before the previous block is converted so that the
 // load latency overlaps the integer work.
@@ -382,9 +371,12 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
     uint32_t aph[2] = {0, 0};
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
       const TileJob jb = jobs.job(tile);
-      const bool wide = jb.tn == TN;  // 128 columns per warp, else 64
+      // a 128-column tile is drained by the warps of the first column half
+      // alone (128 columns each, as for a 256-column tile); the others only
+      // release the accumulator
+      const bool active = jb.tn == TN || h == 0;
       const int row = jb.row + 32 * q + lane;
-      const int col = jb.col + (wide ? 128 : 64) * h;
+      const int col = jb.col + 128 * h;
       int chunk = 0;
       for (int d = 0; d < jb.D; ++d) {
         const int S = mdgi::diag_pairs(d, jb.s) * jb.KB;
@@ -397,29 +389,19 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
           if (!ok) goto epi_done;
           aph[buf] ^= 1;
           fence_after();
-          const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + buf * TN +
-                                 (wide ? 128 : 64) * h;
-          if (wide)
-            drain128(taddr, acc);
-          else
-            drain64(taddr, acc);
+          const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + buf * TN + 128 * h;
+          if (active) drain128(taddr, acc);
           fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(accempty(buf));
           buf ^= 1;
           const int g1 = g0 + mdgi::GROUP_STEPS;
           if (g1 % mdgi::CHUNK_STEPS == 0 || g1 >= S) {
-            int4 *dst = reinterpret_cast<int4 *>(jb.out + (size_t)chunk * jb.plane_c +
-                                                 (size_t)row * jb.Np + col);
-            if (wide) {
+            if (active) {
+              int4 *dst = reinterpret_cast<int4 *>(jb.out + (size_t)chunk * jb.plane_c +
+                                                   (size_t)row * jb.Np + col);
 #pragma unroll
               for (int v = 0; v < 32; ++v) {
-                dst[v] = make_int4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
-                acc[4 * v] = acc[4 * v + 1] = acc[4 * v + 2] = acc[4 * v + 3] = 0;
-              }
-            } else {
-#pragma unroll
-              for (int v = 0; v < 16; ++v) {
                 dst[v] = make_int4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
                 acc[4 * v] = acc[4 * v + 1] = acc[4 * v + 2] = acc[4 * v + 3] = 0;
               }
