@@ -32,7 +32,8 @@
 struct mdg_batch_s {
   int count = 0, nwmax = 4, total_tiles = 0;
   int scale_units = 0, digit_units = 0, renorm_units = 0;
-  int renorm_begin[4] = {0, 0, 0, 0}, renorm_count[4] = {0, 0, 0, 0};  // per P = 2, 4, 8, 16
+  // per P = 2, 4, 8, 16: first output row, rows, widest n
+  int renorm_begin[4] = {0, 0, 0, 0}, renorm_count[4] = {0, 0, 0, 0}, renorm_n[4] = {0, 0, 0, 0};
   int tiles_policy = MDG_BATCH_TILES_AUTO;
   mdgi::BatchProblem *dprobs = nullptr;
   mdgi::GroupedProblem *dgroups = nullptr;
@@ -126,7 +127,7 @@ int plan_batch(const mdg_problem *problems, int count, Layout *L, mdg_batch_s *h
   L->off_chunks.resize(count);
   int scale_u = 0, digit_u = 0, renorm_u = 0, offE = 0, offF = rows;
   h->nwmax = 4;
-  for (int i = 0; i < 4; ++i) h->renorm_begin[i] = h->renorm_count[i] = 0;
+  for (int i = 0; i < 4; ++i) h->renorm_begin[i] = h->renorm_count[i] = h->renorm_n[i] = 0;
   // the table is kept in order of P (stable): blocks of one P sit together
   // in every stage's launch
   std::vector<int> order(count);
@@ -148,10 +149,9 @@ int plan_batch(const mdg_problem *problems, int count, Layout *L, mdg_batch_s *h
     if (!nw || nw > mdgi::batch_words(q.p)) return MDG_ERROR_NOT_SUPPORTED;
     h->nwmax = std::max(h->nwmax, mdgi::batch_words(q.p));
     const int kblocks = (Kp + 127) / 128;
-    const int V = mdgi::batch_cols_per_thread(q.p);
     const int scale_a = (q.m + 7) / 8, scale_b = (q.n + 31) / 32;
     const int digit_a = Mp * kblocks, digit_b = Np * kblocks;
-    const int out_u = q.m * ((q.n + 128 * V - 1) / (128 * V));
+    const int out_u = q.m;  // renormalisation: one row of blocks per output row
     if (ws) {
       BatchProblem b{};
       b.p = q.p; b.s = s; b.D = D; b.m = q.m; b.n = q.n; b.k = q.k;
@@ -172,6 +172,7 @@ int plan_batch(const mdg_problem *problems, int count, Layout *L, mdg_batch_s *h
     const int pi = q.p == 2 ? 0 : q.p == 4 ? 1 : q.p == 8 ? 2 : 3;
     if (h->renorm_count[pi] == 0) h->renorm_begin[pi] = renorm_u;
     h->renorm_count[pi] += out_u;
+    h->renorm_n[pi] = std::max(h->renorm_n[pi], q.n);
     scale_u += scale_a + scale_b;
     digit_u += digit_a + digit_b;
     renorm_u += out_u;
@@ -300,11 +301,11 @@ int mdg_batch_run(mdg_batch_s *h, void *stream) {
   }
 #undef MDG_BATCH_STAGES
   MDG_TRY(mdgi::launch_diag_gemm_grouped(h->dgroups, h->count, h->total_tiles, st));
-  const int *rb = h->renorm_begin, *rc = h->renorm_count;
-  MDG_TRY(mdgi::launch_batch_renorm<2>(h->dprobs, h->count, rb[0], rc[0], h->exps, st));
-  MDG_TRY(mdgi::launch_batch_renorm<4>(h->dprobs, h->count, rb[1], rc[1], h->exps, st));
-  MDG_TRY(mdgi::launch_batch_renorm<8>(h->dprobs, h->count, rb[2], rc[2], h->exps, st));
-  MDG_TRY(mdgi::launch_batch_renorm<16>(h->dprobs, h->count, rb[3], rc[3], h->exps, st));
+  const int *rb = h->renorm_begin, *rc = h->renorm_count, *rn = h->renorm_n;
+  MDG_TRY(mdgi::launch_batch_renorm<2>(h->dprobs, h->count, rb[0], rc[0], rn[0], h->exps, st));
+  MDG_TRY(mdgi::launch_batch_renorm<4>(h->dprobs, h->count, rb[1], rc[1], rn[1], h->exps, st));
+  MDG_TRY(mdgi::launch_batch_renorm<8>(h->dprobs, h->count, rb[2], rc[2], rn[2], h->exps, st));
+  MDG_TRY(mdgi::launch_batch_renorm<16>(h->dprobs, h->count, rb[3], rc[3], rn[3], h->exps, st));
   return MDG_SUCCESS;
 }
 

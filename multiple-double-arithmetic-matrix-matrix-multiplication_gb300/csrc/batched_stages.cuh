@@ -96,25 +96,19 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// Renormalisation of one unit: output row r, 128 V columns.
-template <int P>
-__device__ __forceinline__ void renorm_unit(const BatchProblem &b, const int *exps, int lu) {
-  constexpr int V = batch_cols_per_thread(P);
-  const int nb = (b.n + 128 * V - 1) / (128 * V);
-  const int r = lu / nb, c0 = (lu - r * nb) * 128 * V + V * (int)threadIdx.x;
-  renorm_elems<P, batch_words(P), V>(b.s, b.D, b.Kp / 64, b.m, b.n, b.chunks, b.plane_c, b.Np,
-                                     exps + b.offE, exps + b.offF, b.C, b.ldc, r, c0);
-}
-
-// The renormalisation runs one launch per P: a kernel with the bodies of
-// several widths measured 15 % slower than these (one body each).
+// The renormalisation runs one launch per P (a kernel holding the bodies of
+// several widths measured 15 % slower): block (x, y) takes output row
+// row0 + x of the P group, columns 128 V y .. +128 V - 1.
 template <int P>
 __global__ void __launch_bounds__(128)
     renorm_p(const BatchProblem *__restrict__ pr, int count, const int *__restrict__ exps,
-             int unit0) {
-  const int u = unit0 + (int)blockIdx.x;
-  const BatchProblem &b = pr[find_problem<kRenormUnits>(pr, count, u)];
-  renorm_unit<P>(b, exps, u - b.out_begin);
+             int row0) {
+  constexpr int V = batch_cols_per_thread(P);
+  const int x = row0 + (int)blockIdx.x;
+  const BatchProblem &b = pr[find_problem<kRenormUnits>(pr, count, x)];
+  const int r = x - b.out_begin, c0 = ((int)blockIdx.y * 128 + (int)threadIdx.x) * V;
+  renorm_elems<P, batch_words(P), V>(b.s, b.D, b.Kp / 64, b.m, b.n, b.chunks, b.plane_c, b.Np,
+                                     exps + b.offE, exps + b.offF, b.C, b.ldc, r, c0);
 }
 
 template <int NWMAX>
@@ -135,10 +129,12 @@ int launch_batch_digits(const BatchProblem *pr, int count, int units, const int 
 }
 
 template <int P>
-int launch_batch_renorm(const BatchProblem *pr, int count, int unit0, int units, const int *exps,
-                        cudaStream_t st) {
-  if (units == 0) return MDG_SUCCESS;
-  renorm_p<P><<<units, 128, 0, st>>>(pr, count, exps, unit0);
+int launch_batch_renorm(const BatchProblem *pr, int count, int row0, int rows, int max_n,
+                        const int *exps, cudaStream_t st) {
+  if (rows == 0 || max_n == 0) return MDG_SUCCESS;
+  constexpr int V = batch_cols_per_thread(P);
+  renorm_p<P><<<dim3(rows, ceil_div(ceil_div(max_n, V), 128)), 128, 0, st>>>(pr, count, exps,
+                                                                             row0);
   MDG_TRY_LAUNCH();
   return MDG_SUCCESS;
 }

@@ -27,7 +27,7 @@ __host__ __device__ constexpr int batch_cols_per_thread(int p) {
 //           32 columns of B
 //   digits: Mp x ceil(Kp / 128) blocks of A's digit rows, then
 //           Np x ceil(Kp / 128) of B's
-//   renorm: m x ceil(n / (128 V)) blocks of output rows
+//   renorm: one row of blocks per output row (m rows), per limb count
 struct BatchProblem {
   int p, s, D, m, n, k, Mp, Np, Kp;
   const double *A, *B;
@@ -39,7 +39,7 @@ struct BatchProblem {
   long long plane_a, plane_b, plane_c;
   int scale_begin, scale_b_off;  // first scale unit; units of A's rows
   int dig_begin, dig_b_off;      // first digit unit; units of A's digit rows
-  int out_begin;                 // first renorm unit
+  int out_begin;                 // first output row among those of its P
 };
 
 enum { kScaleUnits = 0, kDigitUnits = 1, kRenormUnits = 2 };
@@ -62,15 +62,15 @@ __device__ __forceinline__ int find_problem(const BatchProblem *pr, int count, i
 // One launch each over every problem of the batch for the exponents and
 // the digits: NWMAX is the widest integer of the batch (4, 6, 10 or 16
 // words, the P of its widest problem); the kernels switch on each problem's
-// P.  The renormalisation: one launch per P over that P's units
-// [unit0, unit0 + units).  (Instantiated in batched_w{4,6,10,16}.cu.)
+// P.  The renormalisation: one launch per P over that P's output rows
+// [row0, row0 + rows), columns up to the widest n of the group.  (Instantiated in batched_w{4,6,10,16}.cu.)
 template <int NWMAX>
 int launch_batch_scale(const BatchProblem *pr, int count, int units, int *exps, cudaStream_t st);
 template <int NWMAX>
 int launch_batch_digits(const BatchProblem *pr, int count, int units, const int *exps,
                         cudaStream_t st);
 template <int P>
-int launch_batch_renorm(const BatchProblem *pr, int count, int unit0, int units, const int *exps,
-                        cudaStream_t st);
+int launch_batch_renorm(const BatchProblem *pr, int count, int row0, int rows, int max_n,
+                        const int *exps, cudaStream_t st);
 
 }  // namespace mdgi

@@ -7,5 +7,5 @@ template int mdgi::launch_batch_scale<16>(const mdgi::BatchProblem *, int, int, 
                                           cudaStream_t);
 template int mdgi::launch_batch_digits<16>(const mdgi::BatchProblem *, int, int, const int *,
                                            cudaStream_t);
-template int mdgi::launch_batch_renorm<16>(const mdgi::BatchProblem *, int, int, int,
+template int mdgi::launch_batch_renorm<16>(const mdgi::BatchProblem *, int, int, int, int,
                                            const int *, cudaStream_t);

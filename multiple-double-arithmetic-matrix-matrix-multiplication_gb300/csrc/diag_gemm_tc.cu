@@ -336,12 +336,16 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
               const uint32_t a_addr = smem_base + st * STAGE_BYTES;
               const uint64_t da = sw128_desc(a_addr), db = sw128_desc(a_addr + A_BYTES);
               // the last k-block of a pair: only the MMAs that reach data
-              const int nsub = (kb == jb.KB - 1) ? jb.ktail : TK / 16;
+              const bool short_block = kb == jb.KB - 1 && jb.ktail < TK / 16;
               if (++kb == jb.KB) kb = 0;
+              if (!short_block) {
 #pragma unroll
-              for (int kk = 0; kk < TK / 16; ++kk)
-                if (kk < nsub)
+                for (int kk = 0; kk < TK / 16; ++kk)
                   mma_bf16_n(dt, da + 2 * kk, db + 2 * kk, idesc, (t > g0 || kk > 0) ? 1u : 0u);
+              } else {
+                for (int kk = 0; kk < jb.ktail; ++kk)
+                  mma_bf16_n(dt, da + 2 * kk, db + 2 * kk, idesc, (t > g0 || kk > 0) ? 1u : 0u);
+              }
               mma_commit(empty(st));
               any = true;
               if (++st == STAGES) {
