@@ -14,9 +14,11 @@ diagonal GEMM on the tensor cores, renormalisation.
            (2 Mp Np Kp per digit pair) over its own event-timed duration
   cpu_baseline  the oracle's plain quad-double GEMM (the C restatement of
            the reference's matmulqdf) on the host cores, a bounded sample
-  forms    the FP64-split and plain forms on the 1024^3 quad-double
-           workload (seed 1), and error bits of every form against the
-           exact product on a sampled block
+  forms    the FP64-split, FP64-digit and plain forms beside the BF16 form
+           on the quad-double 1024^3 (seed 1) and octo-double 2048^3
+           row/column-spread (seed 2) workloads, with error bits of every
+           form against the exact product on sampled entries; a
+           hexa-double line; the FP64 and INT8 tensor rates
 
 --impl reference times the reference's CPU implementation of the path
 (oracle/_ref when it was built from the reference sources on this machine,
@@ -57,7 +59,7 @@ WORKLOADS = {
 DIAG_TRAFFIC_BYTES = {"qd8192_normal": 479.62e9, "qd4096_normal": 74.35e9}
 
 
-DEFAULT_SLICES = {2: 14, 4: 28, 8: 55, 16: 108}
+DEFAULT_SLICES = {2: 14, 4: 28, 8: 55, 16: 110}
 
 
 def digit_pairs(s, D):
@@ -469,6 +471,8 @@ def bench_forms(api, inputs, ex, stream):
                                               sample, iters=3)
         block["fp64split"] = bench_form_line(api, ex, stream, P, A, B, "fp64split", dA, dB,
                                              sample)
+        block["fp64_digits"] = bench_form_line(api, ex, stream, P, A, B, "fp64_digits", dA, dB,
+                                               sample)
         # the plain octo-double GEMM takes ~20 s at 2048^3: rows 0..511 of C
         block["plain"] = bench_form_line(api, ex, stream, P, A, B, "plain", dA, dB, sample,
                                          rows=512 if P >= 8 else None)
@@ -493,7 +497,25 @@ def bench_forms(api, inputs, ex, stream):
                                   "reference's count, TCtest.cu:136-148), issued as unfused "
                                   "mul/add; the DGEMM flop rate stands in for the FP64 "
                                   "CUDA-core peak, which the peaks file does not hold"}
+        fd = block["fp64_digits"]
+        s19 = api.default_slices(P, "fp64_digits")
+        fd_tflops = 2.0 * digit_pairs(s19, s19) * mnk / (fd["ms"] / 1e3) / 1e12
+        fd["digits"] = s19
+        fd["roofline"] = {"bound": "fp64 tensor (DMMA)", "achieved_tflops": fd_tflops,
+                          "peak_tflops": fp64, "frac": fd_tflops / fp64,
+                          "digit_pairs": digit_pairs(s19, s19),
+                          "peak_kind": "cuBLAS DGEMM rate measured in this run"}
         sl = block["slice_bf16"]
+        block["slice_over_fp64_digits"] = {
+            "ratio": sl["gflops"] / fd["gflops"],
+            "equal_accuracy": bool(fd["error_bits_normwise"] >= pl["error_bits_normwise"] - 1 and
+                                   sl["error_bits_normwise"] >= pl["error_bits_normwise"] - 1),
+            "error_bits_normwise": {"slice_bf16": sl["error_bits_normwise"],
+                                    "fp64_digits": fd["error_bits_normwise"],
+                                    "plain": pl["error_bits_normwise"]},
+            "note": "the same exact digit scheme on the FP64 tensor cores (19-bit digits) "
+                    "and on the BF16 ones (8-bit digits): both at or above the plain "
+                    "form's error bits"}
         block["slice_over_fp64split"] = {
             "ratio": sl["gflops"] / sp["gflops"],
             "equal_accuracy": False,
@@ -507,7 +529,7 @@ def bench_forms(api, inputs, ex, stream):
         forms[wl] = block
         del dA, dB
         torch.cuda.empty_cache()
-    # hexa-double: the BF16 form (108 digits, 5886 digit pairs) against the
+    # hexa-double: the BF16 form (110 digits, 6105 digit pairs) against the
     # plain hd GEMM on a 1024 x 1024 x 512 problem (uniform inputs, seed 16)
     rng = np.random.default_rng(16)
     m, n, k = 1024, 1024, 512

@@ -54,13 +54,21 @@ enum {
    * diagonal sums (FP32 accumulation flushed every 256 products into
    * integers), exact rounding back to P limbs.  No reference counterpart:
    * this is the tensor-core form the reference set out to build. */
-  MDG_FORM_SLICE_BF16 = 2
+  MDG_FORM_SLICE_BF16 = 2,
+  /* The same slice-digit scheme on the FP64 tensor cores the reference
+   * uses (DMMA, TCtest.cu:21-46): 19-bit balanced digits stored as doubles
+   * (quad-double: 12 digits, 78 digit pairs), FP64 sums of at most 65536
+   * products (exact), int64 diagonal sums, the same exact rounding.  It
+   * reaches the BF16 form's accuracy, so the two tensor-core paths compare
+   * at equal error bits.  mdg_options.slices / diagonals set its digits
+   * (default mdg_default_fp64_digits). */
+  MDG_FORM_FP64_DIGITS = 3
 };
 
 /* Options; a NULL pointer or zero fields mean the defaults. */
 typedef struct {
-  int slices;       /* BF16 form: digits per operand (0: default for P) */
-  int diagonals;    /* BF16 form: diagonals kept, 1..2*slices-1 (0: = slices) */
+  int slices;       /* digit forms: digits per operand (0: default for P) */
+  int diagonals;    /* digit forms: diagonals kept, 1..2*slices-1 (0: = slices) */
   int split_kind;   /* FP64 form: 0 split4 (pp=4P), 1 split8 (pp=8P), 2 mixed dd (pp=12) */
   int split_exact;  /* FP64 form: 0 or 1 = exact slices (default), 2 = reference-compatible */
   int engine;       /* BF16 form: 0 auto, 1 tcgen05 128x256 tiles, 2 tcgen05 CTA pairs
@@ -87,6 +95,9 @@ int mdg_version(void);
 
 /* Default number of BF16 digits for P limbs. */
 int mdg_default_slices(int p);
+/* Default number of 19-bit digits of MDG_FORM_FP64_DIGITS for P limbs
+ * (6, 12, 24, 47 for P = 2, 4, 8, 16). */
+int mdg_default_fp64_digits(int p);
 
 /* ---------------------------------------------------------------- GEMM -- */
 
@@ -162,7 +173,8 @@ void mdg_batch_destroy(mdg_batch batch);
 enum { MDG_BATCH_TILES_AUTO = 0, MDG_BATCH_TILES_256 = 1, MDG_BATCH_TILES_128 = 2 };
 /* Re-deals the plan's tiles under `policy` (uploads the tile table and
  * synchronises `stream`; not during a capture).  mdg_batch_tiles returns
- * the policy in use. */
+ * the policy in use; a new plan starts with the policy recorded by
+ * mdg_batch_tune for its problem shapes, else MDG_BATCH_TILES_256. */
 int mdg_batch_set_tiles(mdg_batch batch, int policy, void *stream);
 int mdg_batch_tiles(mdg_batch batch);
 /* Times one mdg_batch_run under each tile policy (after a warm-up each),

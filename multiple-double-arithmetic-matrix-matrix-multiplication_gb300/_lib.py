@@ -34,6 +34,7 @@ SIGNATURES = {
     "mdg_last_cuda_error": (c_char_p, []),
     "mdg_version": (c_int, []),
     "mdg_default_slices": (c_int, [c_int]),
+    "mdg_default_fp64_digits": (c_int, [c_int]),
     "mdg_gemm_workspace_size": (c_size, [c_int] * 5 + [_P_OPT]),
     "mdg_gemm": (c_int, [c_int] * 5 + [c_vp, c_int, c_vp, c_int, c_vp, c_int, _P_OPT, c_vp, c_size,
                                         c_vp]),

@@ -14,7 +14,7 @@ import torch
 
 from ._lib import Options, Problem, check, lib
 
-FORMS = {"plain": 0, "fp64split": 1, "slice_bf16": 2}
+FORMS = {"plain": 0, "fp64split": 1, "slice_bf16": 2, "fp64_digits": 3}
 SPLIT_KINDS = {"split4": 0, "split8": 1, "mix": 2}
 
 
@@ -77,7 +77,10 @@ def _dev(x, device="cuda"):
     return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).to(device)
 
 
-def default_slices(p):
+def default_slices(p, form="slice_bf16"):
+    """Default digit count of a digit form for P limbs."""
+    if form == "fp64_digits":
+        return lib().mdg_default_fp64_digits(p)
     return lib().mdg_default_slices(p)
 
 

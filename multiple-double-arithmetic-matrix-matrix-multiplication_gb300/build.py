@@ -29,7 +29,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler",
 # them in parallel; the longest unit then bounds the build.
 SOURCES = ["capi.cu", "plain_gemm.cu", "floatybits.cu", "fp64split.cu", "slice_tc.cu",
            "diag_gemm_tc.cu", "dropin.cu", "noalloc.cu", "batched.cu", "generate.cu",
-           "gemm_ex.cu", "plan.cu", "renorm_p2.cu", "renorm_p4.cu", "renorm_p8.cu", "renorm_p16.cu",
+           "gemm_ex.cu", "plan.cu", "digits64.cu", "renorm_p2.cu", "renorm_p4.cu", "renorm_p8.cu", "renorm_p16.cu",
            "batched_w4.cu", "batched_w6.cu", "batched_w10.cu", "batched_w16.cu"]
 
 

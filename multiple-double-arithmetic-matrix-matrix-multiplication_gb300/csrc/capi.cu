@@ -119,7 +119,7 @@ static DeviceCache g_cache;
 // ---------------------------------------------------------------- checks --
 static int check_gemm_args(int form, int p, int m, int n, int k, const void *A, int lda,
                            const void *B, int ldb, const void *C, int ldc) {
-  if (form < MDG_FORM_PLAIN || form > MDG_FORM_SLICE_BF16) return MDG_ERROR_INVALID_FORM;
+  if (form < MDG_FORM_PLAIN || form > MDG_FORM_FP64_DIGITS) return MDG_ERROR_INVALID_FORM;
   if (!valid_p(p)) return MDG_ERROR_INVALID_LIMBS;
   if (m < 0 || n < 0 || k < 0) return MDG_ERROR_INVALID_SIZE;
   if (lda < std::max(k, 1) || ldb < std::max(n, 1) || ldc < std::max(n, 1))
@@ -133,8 +133,11 @@ struct Opts {
   int slices, diagonals, split_kind, split_exact, engine, parts, raster;
 };
 
-static int resolve_opts(int p, const mdg_options *o, Opts *r) {
-  r->slices = (o && o->slices) ? o->slices : mdg_default_slices(p);
+// Options with the defaults filled in; the digit count and its limits
+// depend on the form (8-bit digits for the BF16 form, 19-bit for FP64).
+static int resolve_opts(int form, int p, const mdg_options *o, Opts *r) {
+  const bool d64 = form == MDG_FORM_FP64_DIGITS;
+  r->slices = (o && o->slices) ? o->slices : d64 ? digits64_default(p) : mdg_default_slices(p);
   r->diagonals = (o && o->diagonals) ? o->diagonals : r->slices;
   r->split_kind = o ? o->split_kind : 0;
   if (o && (o->split_exact < 0 || o->split_exact > 2)) return MDG_ERROR_INVALID_FORM;
@@ -148,7 +151,8 @@ static int resolve_opts(int p, const mdg_options *o, Opts *r) {
   if (r->diagonals < 1 || r->diagonals > 2 * r->slices - 1) return MDG_ERROR_INVALID_FORM;
   if (r->split_kind < 0 || r->split_kind > 2) return MDG_ERROR_INVALID_FORM;
   if (r->split_kind == 2 && p != 2) return MDG_ERROR_INVALID_LIMBS;
-  if (!words_for(r->slices, r->diagonals)) return MDG_ERROR_NOT_SUPPORTED;
+  if (!(d64 ? words64_for(r->slices, r->diagonals) : words_for(r->slices, r->diagonals)))
+    return MDG_ERROR_NOT_SUPPORTED;
   return MDG_SUCCESS;
 }
 
@@ -217,6 +221,7 @@ static int run_split_gemm(int p, const Opts &o, int m, int n, int k, const doubl
 static size_t workspace_bytes(int form, int p, int m, int n, int k, const Opts &o) {
   if (form == MDG_FORM_PLAIN) return 0;
   if (form == MDG_FORM_FP64_SPLIT) return make_split_plan(p, o.split_kind, m, n, k).total;
+  if (form == MDG_FORM_FP64_DIGITS) return make_digits64_plan(p, o.slices, o.diagonals, m, n, k).total;
   return make_slice_plan(p, o.slices, o.diagonals, m, n, k).total;
 }
 
@@ -319,12 +324,14 @@ const char *mdg_last_cuda_error(void) { return g_cuda_error; }
 
 int mdg_version(void) { return 100; }
 
+int mdg_default_fp64_digits(int p) { return digits64_default(p); }
+
 int mdg_default_slices(int p) {
   switch (p) {
     case 2: return 14;
     case 4: return 28;
     case 8: return 55;
-    case 16: return 108;
+    case 16: return 110;  /* 879 bits: above the plain hexa-double GEMM's ~870 */
   }
   return 0;
 }
@@ -332,7 +339,7 @@ int mdg_default_slices(int p) {
 size_t mdg_gemm_workspace_size(int form, int p, int m, int n, int k, const mdg_options *opt) {
   Opts o;
   if (!valid_p(p) || m < 0 || n < 0 || k < 0) return 0;
-  if (resolve_opts(p, opt, &o) != MDG_SUCCESS) return 0;
+  if (resolve_opts(form, p, opt, &o) != MDG_SUCCESS) return 0;
   return workspace_bytes(form, p, m, n, k, o);
 }
 
@@ -341,7 +348,7 @@ int mdg_gemm(int form, int p, int m, int n, int k, const double *A, int lda, con
              size_t workspace_bytes_, void *stream) {
   MDG_TRY(check_gemm_args(form, p, m, n, k, A, lda, B, ldb, C, ldc));
   Opts o;
-  MDG_TRY(resolve_opts(p, opt, &o));
+  MDG_TRY(resolve_opts(form, p, opt, &o));
   cudaStream_t st = as_stream(stream);
   if (m == 0 || n == 0) return MDG_SUCCESS;
   if (k == 0) {  // empty sum: C = 0
@@ -356,6 +363,9 @@ int mdg_gemm(int form, int p, int m, int n, int k, const double *A, int lda, con
   if (!workspace || workspace_bytes_ < need) return MDG_ERROR_WORKSPACE;
   if (form == MDG_FORM_FP64_SPLIT)
     return run_split_gemm(p, o, m, n, k, A, lda, B, ldb, C, ldc, workspace, st);
+  if (form == MDG_FORM_FP64_DIGITS)
+    return run_digits64_gemm(make_digits64_plan(p, o.slices, o.diagonals, m, n, k), A, lda, B,
+                             ldb, C, ldc, workspace, st);
   const SlicePlan pl = make_slice_plan(p, o.slices, o.diagonals, m, n, k);
   if (pl.Mp > 65535 || pl.Np > 65535) return MDG_ERROR_NOT_SUPPORTED;
   return run_slice_gemm(pl, A, lda, B, ldb, C, ldc, workspace, engine_choice(o.engine), o.parts,
@@ -367,7 +377,7 @@ int mdg_gemm_host(int form, int p, int m, int n, int k, const double *A, const d
   MDG_TRY(check_gemm_args(form, p, m, n, k, A, std::max(k, 1), B, std::max(n, 1), C,
                           std::max(n, 1)));
   Opts o;
-  MDG_TRY(resolve_opts(p, opt, &o));
+  MDG_TRY(resolve_opts(form, p, opt, &o));
   if (m == 0 || n == 0) return MDG_SUCCESS;
   const size_t sa = sizeof(double) * (size_t)m * k * p, sb = sizeof(double) * (size_t)k * n * p,
                sc = sizeof(double) * (size_t)m * n * p;

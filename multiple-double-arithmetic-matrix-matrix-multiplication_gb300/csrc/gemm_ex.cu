@@ -115,7 +115,7 @@ ExLayout ex_layout(size_t inner, int trans_a, int trans_b, int accumulate, int p
 int check_ex(int form, int trans_a, int trans_b, int accumulate, int p, int m, int n, int k,
              int lda, int ldb, int ldc) {
   if (!mdgi::valid_p(p)) return MDG_ERROR_INVALID_LIMBS;
-  if (form < MDG_FORM_PLAIN || form > MDG_FORM_SLICE_BF16) return MDG_ERROR_INVALID_FORM;
+  if (form < MDG_FORM_PLAIN || form > MDG_FORM_FP64_DIGITS) return MDG_ERROR_INVALID_FORM;
   if ((trans_a | trans_b | accumulate) & ~1) return MDG_ERROR_INVALID_FORM;
   if (m < 0 || n < 0 || k < 0) return MDG_ERROR_INVALID_SIZE;
   if (lda < std::max(trans_a ? m : k, 1) || ldb < std::max(trans_b ? k : n, 1) ||

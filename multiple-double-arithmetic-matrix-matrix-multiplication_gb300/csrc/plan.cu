@@ -45,7 +45,9 @@ int device_key(std::string *out) {
 }
 
 std::string shape_key(int form, int p, int m, int n, int k, const mdg_options *opt) {
-  const int s = (opt && opt->slices) ? opt->slices : mdg_default_slices(p);
+  const int s = (opt && opt->slices) ? opt->slices
+                : form == MDG_FORM_FP64_DIGITS ? mdg_default_fp64_digits(p)
+                                               : mdg_default_slices(p);
   const int D = (opt && opt->diagonals) ? opt->diagonals : s;
   const mdgi::SlicePlan pl = mdgi::make_slice_plan(p, s, D, m, n, k);
   char buf[160];
@@ -159,7 +161,7 @@ int mdg_plan_create(int form, int p, int m, int n, int k, const mdg_options *opt
                     mdg_plan *plan) {
   if (!plan) return MDG_ERROR_NULL_POINTER;
   *plan = nullptr;
-  if (form < MDG_FORM_PLAIN || form > MDG_FORM_SLICE_BF16) return MDG_ERROR_INVALID_FORM;
+  if (form < MDG_FORM_PLAIN || form > MDG_FORM_FP64_DIGITS) return MDG_ERROR_INVALID_FORM;
   if (!mdgi::valid_p(p)) return MDG_ERROR_INVALID_LIMBS;
   if (m < 0 || n < 0 || k < 0) return MDG_ERROR_INVALID_SIZE;
   const size_t bytes = mdg_gemm_workspace_size(form, p, m, n, k, opt);

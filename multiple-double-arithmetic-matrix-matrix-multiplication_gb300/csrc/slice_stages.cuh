@@ -200,6 +200,47 @@ struct IntV<1> {
   static __device__ __forceinline__ void load(const int *p, int (&x)[1]) { x[0] = *p; }
 };
 
+// The P limbs of W * 2^scale (W a wide integer, consumed): limb l is W,
+// rounded to nearest-even to 53 bits, then removed from W.
+template <int P, int NW>
+__device__ __forceinline__ void emit_limbs(uint64_t (&w)[NW], int scale, double *out) {
+#pragma unroll 1
+  for (int l = 0; l < P; ++l) {
+    const bool neg = (int64_t)w[NW - 1] < 0;
+    uint64_t mag[NW];
+#pragma unroll
+    for (int i = 0; i < NW; ++i) mag[i] = w[i];
+    if (neg) mdgi::wide_neg<NW>(mag);
+    const int tb = mdgi::wide_msb<NW>(mag);
+    if (tb < 0) {
+      out[l] = 0.0;
+      continue;
+    }
+    const int sh = tb > 52 ? tb - 52 : 0;
+    // one 64-bit window from bit sh - 1: the round bit, then the 53 bits
+    // of the limb (tb <= 52: the limb is word 0 itself, nothing to round)
+    const uint64_t x = sh > 0 ? mdgi::wide_bits64<NW>(mag, sh - 1) : (mag[0] << 1);
+    uint64_t mm = (x >> 1) & ((1ull << 53) - 1);
+    if (sh > 0 && (x & 1ull)) {
+      const bool sticky = sh > 1 && mdgi::wide_any_below<NW>(mag, sh - 1);
+      if (sticky || (mm & 1)) mm += 1;
+    }
+    // mm 2^(sh + scale) as a double; with the top bit at 52 (or 53 after
+    // rounding up) and a normal exponent it is assembled from its fields
+    // by integer instructions, otherwise converted and scaled in FP64
+    const bool top = mm >> 53;
+    const uint64_t frac = top ? (mm >> 1) : mm;
+    const int be = sh + scale + 52 + (top ? 1 : 0) + 1023;
+    double val;
+    if ((frac >> 52) == 1 && be >= 1 && be <= 2046)
+      val = __longlong_as_double((long long)(((uint64_t)be << 52) | (frac & ((1ull << 52) - 1))));
+    else
+      val = ldexp((double)mm, sh + scale);
+    out[l] = neg ? -val : val;
+    mdgi::wide_add_shifted<NW>(w, neg ? (int64_t)mm : -(int64_t)mm, sh);
+  }
+}
+
 template <int P, int NW, int V>
 __device__ __forceinline__ void renorm_elems(int s, int D, int KB, int m, int n,
                                              const int *__restrict__ chunks, long long plane_c,
@@ -250,42 +291,7 @@ __device__ __forceinline__ void renorm_elems(int s, int D, int KB, int m, int n,
     mdgi::wide_add_shifted<NW>(w[v], T[v], 8 * (D - 1));
     const int scale = E[r] + F[c] - 14 - 8 * (D - 1);
     double *out = C + ((size_t)r * ldc + c) * P;
-#pragma unroll 1
-    for (int l = 0; l < P; ++l) {
-      const bool neg = (int64_t)w[v][NW - 1] < 0;
-      uint64_t mag[NW];
-#pragma unroll
-      for (int i = 0; i < NW; ++i) mag[i] = w[v][i];
-      if (neg) mdgi::wide_neg<NW>(mag);
-      const int tb = mdgi::wide_msb<NW>(mag);
-      if (tb < 0) {
-        out[l] = 0.0;
-        continue;
-      }
-      const int sh = tb > 52 ? tb - 52 : 0;
-      // one 64-bit window from bit sh - 1: the round bit, then the 53 bits
-      // of the limb (tb <= 52: the limb is word 0 itself, nothing to round)
-      const uint64_t x = sh > 0 ? mdgi::wide_bits64<NW>(mag, sh - 1) : (mag[0] << 1);
-      uint64_t mm = (x >> 1) & ((1ull << 53) - 1);
-      if (sh > 0 && (x & 1ull)) {
-        const bool sticky = sh > 1 && mdgi::wide_any_below<NW>(mag, sh - 1);
-        if (sticky || (mm & 1)) mm += 1;
-      }
-      // mm 2^(sh + scale) as a double; with the top bit at 52 (or 53 after
-      // rounding up) and a normal exponent it is assembled from its fields
-      // by integer instructions, otherwise converted and scaled in FP64
-      const bool top = mm >> 53;
-      const uint64_t frac = top ? (mm >> 1) : mm;
-      const int be = sh + scale + 52 + (top ? 1 : 0) + 1023;
-      double val;
-      if ((frac >> 52) == 1 && be >= 1 && be <= 2046)
-        val = __longlong_as_double(
-            (long long)(((uint64_t)be << 52) | (frac & ((1ull << 52) - 1))));
-      else
-        val = ldexp((double)mm, sh + scale);
-      out[l] = neg ? -val : val;
-      mdgi::wide_add_shifted<NW>(w[v], neg ? (int64_t)mm : -(int64_t)mm, sh);
-    }
+    emit_limbs<P, NW>(w[v], scale, out);
   }
 }
 

@@ -44,6 +44,18 @@ struct SlicePlan {
 SlicePlan make_slice_plan(int p, int s, int D, int m, int n, int k);
 int words_for(int s, int D);
 
+// The FP64-DMMA slice-digit form (digits64.cu): default digits per P
+// (19-bit), integer words, workspace layout and the whole GEMM.
+struct Digits64Plan {
+  int p, s, D, m, n, k;
+  size_t off_rowbits, off_colbits, off_E, off_F, off_dA, off_dB, off_Cd, total;
+};
+int digits64_default(int p);
+int words64_for(int s, int D);
+Digits64Plan make_digits64_plan(int p, int s, int D, int m, int n, int k);
+int run_digits64_gemm(const Digits64Plan &pl, const double *A, int lda, const double *B, int ldb,
+                      double *C, int ldc, void *ws, cudaStream_t st);
+
 int launch_scale_exponents(int p, int m, int n, int k, const double *A, int lda,
                            const double *B, int ldb, unsigned long long *rowbits,
                            unsigned long long *colbits, int *E, int *F, cudaStream_t st);

@@ -71,6 +71,7 @@ def lib():
         L.orc_diag_sums.argtypes = [ctypes.c_int] * 5 + [_ip, _ip, _lp]
         L.orc_renorm_diags.argtypes = [ctypes.c_int] * 4 + [_lp, _ip, _ip, _dp]
         L.orc_gemm_slices.argtypes = [ctypes.c_int] * 6 + [_dp, _dp, _dp]
+        L.orc_gemm_digits.argtypes = [ctypes.c_int] * 6 + [_dp, _dp, _dp]
         L.orc_has_openmp.restype = ctypes.c_int
         L.orc_plane_conv.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
         L.orc_generate.argtypes = [ctypes.c_int] * 4 + [ctypes.c_uint64, ctypes.c_int,
@@ -179,6 +180,15 @@ def gemm_slices(P, s, D, A, B, m, n, k):
     B = _f64(B)
     C = np.zeros((m, n, P), dtype=np.float64)
     lib().orc_gemm_slices(P, s, D, m, n, k, _ptr(A), _ptr(B), _ptr(C))
+    return C
+
+
+def gemm_digits(P, s, D, A, B, m, n, k):
+    """The FP64 digit form (19-bit digits) on the CPU, bit for bit."""
+    A = _f64(A)
+    B = _f64(B)
+    C = np.zeros((m, n, P), dtype=np.float64)
+    lib().orc_gemm_digits(P, s, D, m, n, k, _ptr(A), _ptr(B), _ptr(C))
     return C
 
 

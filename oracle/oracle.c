@@ -741,16 +741,17 @@ static void fixed_point(int P, const double *a, int S, int E, bigint *V) {
   }
 }
 
-/* Balanced base-256 digits of V: d[s-1] .. d[1] from the bottom, each
- * ((V + 128) mod 256) - 128, V <- floor((V + 128) / 256); d[0] = V. */
-static void digits_of(bigint *V, int s, int *d) {
+/* Balanced base-2^b digits of V: d[s-1] .. d[1] from the bottom, each
+ * ((V + h) mod 2^b) - h with h = 2^(b-1), V <- floor((V + h) / 2^b);
+ * d[0] = V.  b = 8 for the BF16 form, 19 for the FP64 digit form. */
+static void digits_of_b(bigint *V, int s, int b, int *d) {
   int i;
-  bigint c128;
-  bi_from_i64_shl(&c128, 128, 0);
+  bigint half;
+  bi_from_i64_shl(&half, (int64_t)1 << (b - 1), 0);
   for (i = s - 1; i >= 1; --i) {
-    bi_add(V, &c128);
-    d[i] = (int)(V->w[0] & 255) - 128;
-    bi_sar(V, 8);
+    bi_add(V, &half);
+    d[i] = (int)(V->w[0] & (((uint64_t)1 << b) - 1)) - (1 << (b - 1));
+    bi_sar(V, b);
   }
   d[0] = (int)(int64_t)V->w[0];
 }
@@ -758,9 +759,18 @@ static void digits_of(bigint *V, int s, int *d) {
 /* Digit planes of A: out[i][r][kk] for i < s (int8 values stored as int32
  * here).  trans = 0: x is m x k (rows scaled by E);  trans = 1: x is k x n
  * (columns scaled by E) and the planes are n x k. */
+static void digits_b(int P, int s, int bits, int rows, int cols, const double *x,
+                     const int *E, int trans, int *out);
+
 void orc_digits(int P, int s, int rows, int cols, const double *x,
                 const int *E, int trans, int *out) {
-  int S = 7 + 8 * (s - 1);
+  digits_b(P, s, 8, rows, cols, x, E, trans, out);
+}
+
+/* The same with b-bit digits, S = (b - 1) + b (s - 1). */
+static void digits_b(int P, int s, int bits, int rows, int cols, const double *x,
+                     const int *E, int trans, int *out) {
+  int S = (bits - 1) + bits * (s - 1);
   int r, c, i, d[512];
   long plane = (long)rows * cols;
   for (r = 0; r < rows; ++r)
@@ -780,7 +790,7 @@ void orc_digits(int P, int s, int rows, int cols, const double *x,
         o = (long)r * cols + c;
       }
       fixed_point(P, a, S, e, &V);
-      digits_of(&V, s, d);
+      digits_of_b(&V, s, bits, d);
       for (i = 0; i < s; ++i) out[i * plane + o] = d[i];
     }
 }
@@ -854,8 +864,17 @@ static void to_limbs(int P, bigint *W, int scale, double *out) {
   }
 }
 
+static void renorm_diags_b(int P, int D, int bits, int m, int n, const int64_t *Cd,
+                           const int *E, const int *F, double *C);
+
 void orc_renorm_diags(int P, int D, int m, int n, const int64_t *Cd,
                       const int *E, const int *F, double *C) {
+  renorm_diags_b(P, D, 8, m, n, Cd, E, F, C);
+}
+
+/* W = sum_d C_d 2^(b (D-1-d)), times 2^(E + F - 2 (b - 1) - b (D - 1)). */
+static void renorm_diags_b(int P, int D, int bits, int m, int n, const int64_t *Cd,
+                           const int *E, const int *F, double *C) {
   long pc = (long)m * n;
   int r, c, d;
   for (r = 0; r < m; ++r)
@@ -865,25 +884,42 @@ void orc_renorm_diags(int P, int D, int m, int n, const int64_t *Cd,
       for (d = 0; d < D; ++d) {
         int64_t v = Cd[d * pc + (long)r * n + c];
         if (!v) continue;
-        bi_from_i64_shl(&t, v, 8 * (D - 1 - d));
+        bi_from_i64_shl(&t, v, bits * (D - 1 - d));
         bi_add(&W, &t);
       }
-      to_limbs(P, &W, E[r] + F[c] - 14 - 8 * (D - 1), C + ((long)r * n + c) * P);
+      to_limbs(P, &W, E[r] + F[c] - 2 * (bits - 1) - bits * (D - 1),
+               C + ((long)r * n + c) * P);
     }
 }
+
+static void gemm_digits_b(int P, int s, int D, int bits, int m, int n, int k,
+                          const double *A, const double *B, double *C);
 
 /* Whole slice-digit GEMM on the CPU, for small sizes. */
 void orc_gemm_slices(int P, int s, int D, int m, int n, int k,
                      const double *A, const double *B, double *C) {
+  gemm_digits_b(P, s, D, 8, m, n, k, A, B, C);
+}
+
+/* The FP64 digit form: the same scheme with 19-bit digits (the library's
+ * MDG_FORM_FP64_DIGITS).  Its digit products are summed exactly, so the
+ * result does not depend on the order of the FP64 tensor-core sums. */
+void orc_gemm_digits(int P, int s, int D, int m, int n, int k,
+                     const double *A, const double *B, double *C) {
+  gemm_digits_b(P, s, D, 19, m, n, k, A, B, C);
+}
+
+static void gemm_digits_b(int P, int s, int D, int bits, int m, int n, int k,
+                          const double *A, const double *B, double *C) {
   int *E = (int *)malloc(sizeof(int) * m), *F = (int *)malloc(sizeof(int) * n);
   int *dA = (int *)malloc(sizeof(int) * (size_t)s * m * k);
   int *dB = (int *)malloc(sizeof(int) * (size_t)s * n * k);
   int64_t *Cd = (int64_t *)malloc(sizeof(int64_t) * (size_t)D * m * n);
   orc_scale_exps(P, m, n, k, A, B, E, F);
-  orc_digits(P, s, m, k, A, E, 0, dA);
-  orc_digits(P, s, n, k, B, F, 1, dB);
+  digits_b(P, s, bits, m, k, A, E, 0, dA);
+  digits_b(P, s, bits, n, k, B, F, 1, dB);
   orc_diag_sums(s, D, m, n, k, dA, dB, Cd);
-  orc_renorm_diags(P, D, m, n, Cd, E, F, C);
+  renorm_diags_b(P, D, bits, m, n, Cd, E, F, C);
   free(E);
   free(F);
   free(dA);

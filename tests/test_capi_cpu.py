@@ -35,8 +35,13 @@ def test_status_strings(L):
 
 
 def test_default_slices(L):
-    assert [L.mdg_default_slices(p) for p in (2, 4, 8, 16)] == [14, 28, 55, 108]
+    assert [L.mdg_default_slices(p) for p in (2, 4, 8, 16)] == [14, 28, 55, 110]
     assert L.mdg_default_slices(3) == 0
+    assert [L.mdg_default_fp64_digits(p) for p in (2, 4, 8, 16)] == [6, 12, 24, 47]
+    # the FP64 digit form's workspace: digit planes (8 B a digit), int64
+    # diagonal sums, exponents
+    ws = L.mdg_gemm_workspace_size(3, 4, 100, 80, 60, None)
+    assert ws >= 12 * (100 + 80) * 60 * 8 + 12 * 100 * 80 * 8
 
 
 @pytest.mark.parametrize("p", [0, 1, 3, 5, 32, -2])

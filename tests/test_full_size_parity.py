@@ -66,6 +66,24 @@ def test_slice_form_full_size_block_bit_exact(api, orc, inputs, name):
     assert np.array_equal(np.signbit(got), np.signbit(want))
 
 
+@pytest.mark.parametrize("name", ["dd64", "qd1024", "od2048_spread"])
+def test_fp64_digit_form_full_size_block_bit_exact(api, orc, inputs, name):
+    """The FP64 DMMA digit form on the whole workload; its exponents and
+    digits are per row / column like the BF16 form's, so the sampled block
+    equals the oracle on the block's rows and columns bit for bit."""
+    P, A, B = inputs.workload(name)
+    m, k = A.shape[:2]
+    n = B.shape[1]
+    s = api.default_slices(P, "fp64_digits")
+    C = api.gemm(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda(), "fp64_digits")
+    rows, cols = sample(8, m, 41), sample(8, n, 43)
+    got = C.cpu().numpy()[np.ix_(rows, cols)]
+    del C
+    torch.cuda.empty_cache()
+    Ab, Bb = block_inputs(A, B, rows, cols)
+    assert np.array_equal(got, orc.gemm_digits(P, s, s, Ab, Bb, len(rows), len(cols), k)), name
+
+
 @pytest.mark.parametrize("name", ["dd64", "qd1024"])
 def test_plain_form_full_size_block_bit_exact(api, orc, inputs, name):
     P, A, B = inputs.workload(name)

@@ -187,7 +187,7 @@ def test_fp64split_reference_compatible_mode(api, orc, inputs):
 
 # --------------------------------------------------------- slice digits --
 
-@pytest.mark.parametrize("P,s", [(2, 14), (4, 28), (8, 55), (16, 108)])
+@pytest.mark.parametrize("P,s", [(2, 14), (4, 28), (8, 55), (16, 110)])
 def test_digit_stages_bit_exact(api, orc, inputs, P, s):
     rng = np.random.default_rng(s)
     m, n, k = 20, 13, 37
@@ -229,7 +229,7 @@ def test_diagonal_gemm_exact(api, orc, engine, s, D, k, m, n, monkeypatch):
     assert api.device_status() == 0
 
 
-@pytest.mark.parametrize("P,D", [(2, 14), (4, 28), (8, 55), (16, 108)])
+@pytest.mark.parametrize("P,D", [(2, 14), (4, 28), (8, 55), (16, 110)])
 @pytest.mark.parametrize("k", [64, 64 * 2048])
 def test_renorm_bit_exact(api, orc, P, D, k):
     rng = np.random.default_rng(P + k)
@@ -266,6 +266,37 @@ def test_slice_gemm_bit_exact_against_oracle(api, orc, inputs, engine, P, shape,
     s = api.default_slices(P)
     got = host(api.gemm(dev(A), dev(B), "slice_bf16"))
     assert np.array_equal(got, orc.gemm_slices(P, s, s, A, B, m, n, k))
+
+
+@pytest.mark.parametrize("P", [2, 4, 8, 16])
+@pytest.mark.parametrize("shape", [(1, 1, 1), (33, 31, 70), (130, 129, 65), (3, 5, 70003)])
+def test_fp64_digit_form_bit_exact_against_oracle(api, orc, inputs, P, shape):
+    """The FP64 DMMA digit form (19-bit digits): bit for bit the oracle's
+    restatement.  k = 70003 runs past one 65536-product FP64 segment, so
+    the int64 flush of the DMMA sums is exercised."""
+    m, n, k = shape
+    if P == 16 and m * n * k > 3e5:
+        pytest.skip("hexa-double oracle cost")
+    rng = np.random.default_rng(m + n + k + P + 7)
+    A = inputs.uniform_pd(rng, (m, k), P)
+    B = inputs.uniform_pd(rng, (k, n), P)
+    A, _ = inputs.scale_rows(rng, A, -20, 20)
+    s = api.default_slices(P, "fp64_digits")
+    got = host(api.gemm(dev(A), dev(B), "fp64_digits"))
+    assert np.array_equal(got, orc.gemm_digits(P, s, s, A, B, m, n, k))
+
+
+@pytest.mark.parametrize("name", ["dd64", "qd1024", "od2048_spread"])
+def test_fp64_digit_form_error_bits_not_worse_than_plain(api, inputs, name):
+    ex = pkg("errors")
+    P, A, B = inputs.workload(name, 48, 48, 96)
+    Cd = host(api.gemm(dev(A), dev(B), "fp64_digits"))
+    Cp = host(api.gemm(dev(A), dev(B), "plain"))
+    rows, cols = range(0, 48, 3), range(0, 48, 5)
+    ed = ex.error_bits(Cd, A, B, rows, cols)
+    ep = ex.error_bits(Cp, A, B, rows, cols)
+    print(name, "fp64_digits", ed, "plain", ep)
+    assert ed[1] >= ep[1] - 1.0
 
 
 def test_slice_gemm_schedules_bit_identical(api, inputs, monkeypatch):
@@ -310,13 +341,13 @@ def test_bounded_wait_timeout_is_reported_and_context_survives(api, orc, inputs,
 
 
 def test_slice_gemm_hexa_double_bit_exact(api, orc, inputs):
-    """P = 16 through the BF16 form (108 digits, 5886 digit pairs)."""
+    """P = 16 through the BF16 form (110 digits, 6105 digit pairs)."""
     rng = np.random.default_rng(16)
     m, n, k = 9, 7, 20
     A = inputs.uniform_pd(rng, (m, k), 16)
     B = inputs.uniform_pd(rng, (k, n), 16)
     got = host(api.gemm(dev(A), dev(B), "slice_bf16"))
-    assert np.array_equal(got, orc.gemm_slices(16, 108, 108, A, B, m, n, k))
+    assert np.array_equal(got, orc.gemm_slices(16, 110, 110, A, B, m, n, k))
 
 
 @pytest.mark.parametrize("name", ["dd64", "qd1024", "od2048_spread"])
@@ -530,8 +561,8 @@ def test_batched_tile_policies_bit_identical_and_tuned(api, orc, inputs):
            for P, m, n, k in probs]
     want = [api.gemm(A, B, "slice_bf16") for A, B in ops]
     plan = api.BatchPlan(ops)
-    assert plan.tiles == "auto"
-    for policy in ("256", "128", "auto"):
+    assert plan.tiles == "256"
+    for policy in ("auto", "128", "256"):
         plan.set_tiles(policy)
         for C in plan.Cs:
             C.fill_(np.nan)

@@ -13,7 +13,7 @@ import pytest
 
 from conftest import pkg
 
-SLICES = {2: 14, 4: 28, 8: 55, 16: 108}
+SLICES = {2: 14, 4: 28, 8: 55, 16: 110}
 
 
 def floor_scaled(v, shift):
@@ -122,3 +122,44 @@ def test_slice_form_not_less_accurate_than_plain(orc, inputs, P, dist):
     _, plain_bits = ex.error_bits(orc.gemm_plain(P, A, B, m, n, k), A, B, range(m), range(n))
     assert slice_bits >= plain_bits - 1.0, (slice_bits, plain_bits)
     assert slice_bits > {2: 95, 4: 205, 8: 415}[P]
+
+
+DIGITS19 = {2: 6, 4: 12, 8: 24, 16: 47}
+
+
+@pytest.mark.parametrize("P", [2, 4, 8])
+@pytest.mark.parametrize("dist", ["uniform", "normal", "spread"])
+def test_fp64_digit_form_not_less_accurate_than_plain(orc, inputs, P, dist):
+    """The FP64 digit form (19-bit digits, the library's default counts)
+    keeps at least the plain form's normwise bits against the exact
+    product, like the BF16 digit form."""
+    ex = pkg("errors")
+    rng = np.random.default_rng(60 + P)
+    m = n = k = 12
+    gen = inputs.normal_pd if dist == "normal" else inputs.uniform_pd
+    A = gen(rng, (m, k), P)
+    B = inputs.uniform_pd(rng, (k, n), P)
+    if dist == "spread":
+        A, _ = inputs.scale_rows(rng, A)
+        B, _ = inputs.scale_cols(rng, B)
+    s = DIGITS19[P]
+    _, bits = ex.error_bits(orc.gemm_digits(P, s, s, A, B, m, n, k), A, B, range(m), range(n))
+    _, plain_bits = ex.error_bits(orc.gemm_plain(P, A, B, m, n, k), A, B, range(m), range(n))
+    assert bits >= plain_bits - 1.0, (bits, plain_bits)
+
+
+@pytest.mark.parametrize("P", [2, 4])
+def test_digit_width_does_not_matter_without_truncation(orc, P):
+    """With inputs short enough that neither digit form truncates anything
+    (integers of a few bits), both forms return the exact product: the same
+    bits whatever the digit width."""
+    rng = np.random.default_rng(P + 90)
+    m, n, k = 4, 5, 6
+    A = np.zeros((m, k, P)); B = np.zeros((k, n, P))
+    A[..., 0] = rng.integers(-7, 8, size=(m, k))
+    B[..., 0] = rng.integers(-7, 8, size=(k, n))
+    s8, s19 = SLICES[P], DIGITS19[P]
+    C8 = orc.gemm_slices(P, s8, s8, A, B, m, n, k)
+    C19 = orc.gemm_digits(P, s19, s19, A, B, m, n, k)
+    exact = A[..., 0] @ B[..., 0]
+    assert np.array_equal(C8[..., 0], exact) and np.array_equal(C19, C8)
