@@ -321,18 +321,26 @@ def pipelined_e2e(api, hA, hB, hC, P, m, n, k, ws_bytes, steps):
     return dt
 
 
-def batched_tile_work(probs, slices):
+def batched_tile_work(probs, slices, policy="256"):
     """BF16 FLOP of the batched diagonal GEMM at the given digit counts per
     P: useful (2 m n k per digit pair of the s diagonals kept) and as the
-    grouped kernel pads it (rows to 128, columns to 256, k to 64)."""
+    grouped kernel pads it (rows to 128, columns to the tile width of the
+    policy, k to 16: the last 64-deep block issues only the MMAs that reach
+    data)."""
     def pairs(s):
         return sum(min(d, s - 1) - max(0, d - (s - 1)) + 1 for d in range(s))
     up = lambda x, a: -(-x // a) * a
+    def width(n):
+        if policy == "256":
+            return up(n, 256)
+        if policy == "128":
+            return up(n, 128)
+        return min(up(n, 128), up(n, 256))
     useful = padded = 0.0
     for P, m, n, k in probs:
         q = pairs(slices[P])
         useful += 2.0 * m * n * k * q
-        padded += 2.0 * up(m, 128) * up(n, 256) * up(k, 64) * q
+        padded += 2.0 * up(m, 128) * width(n) * up(k, 16) * q
     return useful, padded
 
 
@@ -345,11 +353,11 @@ def bench_batched(api, inputs, stream):
     ops = inputs.batched_operands(probs, rng)
     dev_ops = [(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()) for A, B in ops]
     flops = sum(2.0 * m * n * k for _, m, n, k in probs)
-    useful, padded = batched_tile_work(probs, {P: api.default_slices(P)
-                                               for P in {pr[0] for pr in probs}})
 
-    def captured(pairs):
+    def captured(pairs, tune=False):
         plan = api.BatchPlan(pairs)
+        if tune:
+            plan.tune()  # tile policy: times 256-, auto- and 128-column tiles
         plan.run()
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
@@ -363,8 +371,11 @@ def bench_batched(api, inputs, stream):
         torch.cuda.synchronize()
         return plan, g
 
-    plan, g = captured(dev_ops)
+    plan, g = captured(dev_ops, tune=True)
     t_graph = event_time(g.replay, torch.cuda.current_stream(), iters=5)
+    policy = plan.tiles
+    useful, padded = batched_tile_work(probs, {P: api.default_slices(P)
+                                               for P in {pr[0] for pr in probs}}, policy)
     # the metric per P (each P's problems as their own graph-replayed plan)
     per_p = {}
     for P in (2, 4, 8):
@@ -394,16 +405,18 @@ def bench_batched(api, inputs, stream):
             "md_gflop": flops / 1e9,
             "slice_graph_gflops": flops / t_graph / 1e9, "slice_graph_ms": t_graph * 1e3,
             "per_p": per_p,
-            # kernels per plan run: row and column maxima, exponents, then two
-            # digit kernels and one renormalisation per limb count, and the
-            # grouped diagonal GEMM (plus one memset of the maxima)
-            "slice_launches_per_batch": 3 + 3 * len({pr[0] for pr in probs}) + 1,
+            # kernels per plan run: exponents of all rows and columns, digits
+            # of all operands, the grouped diagonal GEMM, and one
+            # renormalisation per limb count present
+            "slice_launches_per_batch": 3 + len({pr[0] for pr in probs}),
+            "tile_policy": policy,
             "plain_loop_gflops": flops / t_loop / 1e9, "plain_loop_ms": t_loop * 1e3,
             "plain_batched_gflops": flops / t_pb / 1e9, "plain_batched_ms": t_pb * 1e3,
             "slice_equals_single_problem": bool(same),
             "diag_bf16_tflop": {"useful": useful / 1e12, "padded": padded / 1e12,
                                 "useful_frac": useful / padded,
-                                "tiles": "128 x 256 x 64 (grouped single-CTA kernel)"}}
+                                "tiles": f"128 x {policy} columns (tuned policy), k padded to "
+                                         "16 (grouped single-CTA kernel)"}}
 
 
 # FP64 operations per multi-double multiply-add of the plain form, the
