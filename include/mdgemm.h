@@ -76,7 +76,8 @@ typedef struct {
   int parts;        /* BF16 form, CTA pairs: diagonal ranges per tile (0: auto, 1..8) */
   int raster;       /* BF16 form, CTA pairs: tile order runs across strips this many
                        256-column blocks wide (0: auto) */
-  int reserved;
+  int pace;         /* BF16 form, CTA pairs: cross-cluster pacing window in k-steps
+                       (0: default 64, or MDG_TC_PACE when set; -1: off; at most 65536) */
 } mdg_options;
 
 /* One problem of a batched call. */
@@ -292,7 +293,8 @@ int mdg_renorm_diagonals(int p, int s, int D, int k, int m, int n,
 /* A plan for one problem shape: it owns its device workspace and the
  * schedule it runs with.  mdg_plan_tune times the schedules that give the
  * same bits (BF16 form: CTA pairs with diagonal ranges per tile auto / 1 /
- * 2 / 4, and the single-CTA engine) on the caller's operands, keeps the
+ * 2 / 4, tile strips 4 or 16 column blocks wide, pacing windows 32 or 128
+ * k-steps or none, and the single-CTA engine) on the caller's operands, keeps the
  * fastest, and records it in the library's tuning cache under the device
  * (GPU name and driver version) and the shape class (form, P, digits,
  * padded m, n, k); plans created later for the same class start from the
@@ -308,11 +310,12 @@ int mdg_plan_tune(mdg_plan plan, const double *A, int lda, const double *B, int 
                   double *C, int ldc, void *stream);
 int mdg_plan_run(mdg_plan plan, const double *A, int lda, const double *B, int ldb,
                  double *C, int ldc, void *stream);
-/* The options the plan runs with (engine, parts, raster filled in). */
+/* The options the plan runs with (engine, parts, raster, pace filled in). */
 int mdg_plan_schedule(mdg_plan plan, mdg_options *out);
 void mdg_plan_destroy(mdg_plan plan);
 /* The tuning cache: {"<gpu>|<driver>": {"<form> <p> <s> <D> <Mp> <Np> <Kp>":
- * {"engine": e, "parts": q, "raster": r, "ms": t}, ...}, ...}.  Loading
+ * {"engine": e, "parts": q, "raster": r, "pace": w, "ms": t}, ...}, ...}, and
+ * batched plans under "batch <count> <hash>": {"tiles": policy, "ms": t}.  Loading
  * merges into the cache; MDG_ERROR_NOT_SUPPORTED if the file cannot be
  * opened, MDG_ERROR_INVALID_FORM if it is not of that form. */
 int mdg_tune_cache_load(const char *path);

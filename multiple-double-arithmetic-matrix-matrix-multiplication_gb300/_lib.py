@@ -17,7 +17,7 @@ c_int, c_ll, c_size, c_vp, c_char_p = (ctypes.c_int, ctypes.c_longlong, ctypes.c
 class Options(ctypes.Structure):
     _fields_ = [("slices", c_int), ("diagonals", c_int), ("split_kind", c_int),
                 ("split_exact", c_int), ("engine", c_int), ("parts", c_int),
-                ("raster", c_int), ("reserved", c_int)]
+                ("raster", c_int), ("pace", c_int)]
 
 
 class Problem(ctypes.Structure):

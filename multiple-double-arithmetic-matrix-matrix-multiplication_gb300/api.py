@@ -22,8 +22,9 @@ ENGINES = {"auto": 0, "tc": 1, "tc_pair": 2, "mma_sync": 3}
 
 
 def _opts(slices=0, diagonals=0, split_kind="split4", split_exact=True, engine="auto", parts=0,
-          raster=0):
+          raster=0, pace=0):
     o = Options()
+    o.pace = int(pace)
     o.slices, o.diagonals = int(slices), int(diagonals)
     o.engine = ENGINES[engine] if isinstance(engine, str) else int(engine)
     o.parts = int(parts)

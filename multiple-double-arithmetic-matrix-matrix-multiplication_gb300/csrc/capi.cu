@@ -130,7 +130,7 @@ static int check_gemm_args(int form, int p, int m, int n, int k, const void *A, 
 }
 
 struct Opts {
-  int slices, diagonals, split_kind, split_exact, engine, parts, raster;
+  int slices, diagonals, split_kind, split_exact, engine, parts, raster, pace;
 };
 
 // Options with the defaults filled in; the digit count and its limits
@@ -145,7 +145,9 @@ static int resolve_opts(int form, int p, const mdg_options *o, Opts *r) {
   r->engine = o ? o->engine : 0;
   r->parts = o ? o->parts : 0;
   r->raster = o ? o->raster : 0;
-  if (r->engine < 0 || r->engine > 3 || r->parts < 0 || r->parts > 8 || r->raster < 0)
+  r->pace = o ? o->pace : 0;
+  if (r->engine < 0 || r->engine > 3 || r->parts < 0 || r->parts > 8 || r->raster < 0 ||
+      r->pace < -1 || r->pace > 65536)
     return MDG_ERROR_INVALID_FORM;
   if (r->slices < 1 || r->slices > 128) return MDG_ERROR_INVALID_FORM;
   if (r->diagonals < 1 || r->diagonals > 2 * r->slices - 1) return MDG_ERROR_INVALID_FORM;
@@ -289,7 +291,7 @@ static int host_slice_panels_issue(int p, const Opts &o, int m, int n, int k, co
     }
     MDG_TRY_CUDA(cudaStreamWaitEvent(sc, evA[i], 0));
     MDG_TRY(slice_panel(pl, rows, dA + r0 * ea, k, dC + r0 * ec, n, ws, engine, o.parts, o.raster,
-                        sc));
+                        sc, o.pace));
     MDG_TRY_CUDA(cudaEventRecord(evC[i], sc));
     MDG_TRY_CUDA(cudaStreamWaitEvent(so, evC[i], 0));
     MDG_TRY_CUDA(cudaMemcpyAsync(C + r0 * ec, dC + r0 * ec, row_c * rows, cudaMemcpyDeviceToHost,
@@ -369,7 +371,7 @@ int mdg_gemm(int form, int p, int m, int n, int k, const double *A, int lda, con
   const SlicePlan pl = make_slice_plan(p, o.slices, o.diagonals, m, n, k);
   if (pl.Mp > 65535 || pl.Np > 65535) return MDG_ERROR_NOT_SUPPORTED;
   return run_slice_gemm(pl, A, lda, B, ldb, C, ldc, workspace, engine_choice(o.engine), o.parts,
-                        o.raster, st);
+                        o.raster, st, o.pace);
 }
 
 int mdg_gemm_host(int form, int p, int m, int n, int k, const double *A, const double *B,

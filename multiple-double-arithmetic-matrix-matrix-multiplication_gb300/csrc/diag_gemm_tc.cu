@@ -904,7 +904,7 @@ namespace mdgi {
 int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, const void *dB,
                         int ld, long long plane_a, long long plane_b, int *chunks,
                         long long plane_c, int single, int parts_opt, int raster_opt,
-                        cudaStream_t st) {
+                        cudaStream_t st, int pace_opt) {
   if (Mp % TM || Np % TN || Kp % TK || ld != Kp) return MDG_ERROR_INVALID_SIZE;
   if (plane_a != (long long)Mp * Kp || plane_b != (long long)Np * Kp) return MDG_ERROR_INVALID_SIZE;
   if ((reinterpret_cast<uintptr_t>(dA) | reinterpret_cast<uintptr_t>(dB)) & 15)
@@ -960,6 +960,8 @@ int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, co
     // as "not started"
     int pace = kDefaultPace;
     if (const char *e = std::getenv("MDG_TC_PACE")) pace = std::max(0, std::atoi(e));
+    if (pace_opt > 0) pace = pace_opt;
+    if (pace_opt < 0) pace = 0;
     static std::atomic<uint32_t> epochs{0};
     uint32_t epoch = ++epochs;
     if (epoch == 0) epoch = ++epochs;

@@ -4,7 +4,9 @@
 // A plan owns its device workspace and the mdg_options it runs with.  For
 // the BF16 slice-digit form, mdg_plan_tune times the schedules that return
 // the same bits (the CTA-pair engine with 0 = auto, 1, 2 or 4 diagonal ranges
-// per tile, and the single-CTA engine) on the caller's own operands and keeps
+// per tile, tile strips 4 or 16 column blocks wide, pacing windows of 32 and
+// 128 k-steps or none, and the single-CTA engine) on the caller's own
+// operands and keeps
 // the fastest.  Choices live in a process-wide cache keyed by device ("<GPU
 // name>|<driver version>") and shape class ("<form> <P> <s> <D> <Mp> <Np>
 // <Kp>", the padded sizes the kernels see); mdg_tune_cache_save / _load keep
@@ -24,10 +26,10 @@
 
 namespace {
 
-// A single-problem schedule (engine, parts, raster), or for a batched plan
-// ("batch ..." keys) its tile policy.
+// A single-problem schedule (engine, parts, raster, pace), or for a batched
+// plan ("batch ..." keys) its tile policy.
 struct TuneEntry {
-  int engine = 0, parts = 0, raster = 0, tiles = 0;
+  int engine = 0, parts = 0, raster = 0, pace = 0, tiles = 0;
   double ms = 0.0;
 };
 
@@ -185,6 +187,7 @@ int mdg_plan_create(int form, int p, int m, int n, int k, const mdg_options *opt
         h->opt.engine = e->second.engine;
         h->opt.parts = e->second.parts;
         h->opt.raster = e->second.raster;
+        h->opt.pace = e->second.pace;
       }
     }
   }
@@ -223,8 +226,11 @@ int mdg_plan_tune(mdg_plan plan, const double *A, int lda, const double *B, int 
   }
   mdgi::NvtxRange range("mdg plan tune");
   // schedules with the same bits: CTA pairs (engine 2) with parts auto / 1 /
-  // 2 / 4, and single CTAs (engine 1)
-  const int cand[5][2] = {{2, 0}, {2, 1}, {2, 2}, {2, 4}, {1, 0}};
+  // 2 / 4, tile strips of 4 and 16 column blocks, pacing windows 32, 128 and
+  // off, and single CTAs (engine 1): {engine, parts, raster, pace}
+  const int cand[10][4] = {{2, 0, 0, 0},  {2, 1, 0, 0},   {2, 2, 0, 0},  {2, 4, 0, 0},
+                           {2, 0, 4, 0},  {2, 0, 16, 0},  {2, 0, 0, 32}, {2, 0, 0, 128},
+                           {2, 0, 0, -1}, {1, 0, 0, 0}};
   cudaStream_t st = mdgi::as_stream(stream);
   cudaEvent_t e0, e1;
   MDG_TRY_CUDA(cudaEventCreate(&e0));
@@ -236,6 +242,8 @@ int mdg_plan_tune(mdg_plan plan, const double *A, int lda, const double *B, int 
     mdg_options o = plan->opt;
     o.engine = c[0];
     o.parts = c[1];
+    o.raster = c[2];
+    o.pace = c[3];
     status = mdg_gemm(plan->form, plan->p, plan->m, plan->n, plan->k, A, lda, B, ldb, C, ldc, &o,
                       plan->ws, plan->bytes, stream);  // warm-up
     if (status != MDG_SUCCESS) break;
@@ -266,6 +274,7 @@ int mdg_plan_tune(mdg_plan plan, const double *A, int lda, const double *B, int 
     t.engine = best.engine;
     t.parts = best.parts;
     t.raster = best.raster;
+    t.pace = best.pace;
     t.ms = best_ms;
   }
   return MDG_SUCCESS;
@@ -305,6 +314,7 @@ int mdg_tune_cache_load(const char *path) {
         if (field == "engine") return whole_in(v, 0, 3, &e.engine);
         if (field == "parts") return whole_in(v, 0, 8, &e.parts);
         if (field == "raster") return whole_in(v, 0, 1 << 20, &e.raster);
+        if (field == "pace") return whole_in(v, -1, 65536, &e.pace);
         if (field == "tiles") return whole_in(v, 0, 2, &e.tiles);
         if (field == "ms") {
           if (!(v >= 0.0 && v <= 1e12)) return false;
@@ -341,8 +351,10 @@ int mdg_tune_cache_save(const char *path) {
                         e.second.ms);
         else
           std::snprintf(buf, sizeof(buf),
-                        "{\"engine\": %d, \"parts\": %d, \"raster\": %d, \"ms\": %.4f}",
-                        e.second.engine, e.second.parts, e.second.raster, e.second.ms);
+                        "{\"engine\": %d, \"parts\": %d, \"raster\": %d, \"pace\": %d, "
+                        "\"ms\": %.4f}",
+                        e.second.engine, e.second.parts, e.second.raster, e.second.pace,
+                        e.second.ms);
         out += (first ? "\n    " : ",\n    ") + quoted(e.first) + ": " + buf;
         first = false;
       }

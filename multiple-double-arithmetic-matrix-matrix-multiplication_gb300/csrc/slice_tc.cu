@@ -356,7 +356,7 @@ int slice_prepare_b(const SlicePlan &pl, const double *B, int ldb, void *ws, cud
 }
 
 int slice_panel(const SlicePlan &pl, int rows, const double *A, int lda, double *C, int ldc,
-                void *ws, int engine, int parts, int raster, cudaStream_t st) {
+                void *ws, int engine, int parts, int raster, cudaStream_t st, int pace) {
   if (rows <= 0) return MDG_SUCCESS;
   if (rows > pl.m) return MDG_ERROR_INVALID_SIZE;
   char *base = reinterpret_cast<char *>(ws);
@@ -375,7 +375,8 @@ int slice_panel(const SlicePlan &pl, int rows, const double *A, int lda, double 
                         pl.Kp, st));
   if (engine != 0) {
     MDG_TRY(launch_diag_gemm_tc(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
-                                pl.plane_b, Cd, pl.plane_c, engine == 2 ? 1 : 0, parts, raster, st));
+                                pl.plane_b, Cd, pl.plane_c, engine == 2 ? 1 : 0, parts, raster, st,
+                                pace));
   } else {
     MDG_TRY(launch_diag_gemm_v0(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
                                 pl.plane_b, Cd, pl.plane_c, st));
@@ -386,7 +387,7 @@ int slice_panel(const SlicePlan &pl, int rows, const double *A, int lda, double 
 
 int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *B, int ldb,
                    double *C, int ldc, void *ws, int engine, int parts, int raster,
-                   cudaStream_t st) {
+                   cudaStream_t st, int pace) {
   char *base = reinterpret_cast<char *>(ws);
   auto *rowbits = reinterpret_cast<unsigned long long *>(base + pl.off_rowbits);
   auto *colbits = reinterpret_cast<unsigned long long *>(base + pl.off_colbits);
@@ -408,7 +409,8 @@ int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *
   NvtxRange r2("diagonal GEMM and renormalisation");
   if (engine != 0) {
     MDG_TRY(launch_diag_gemm_tc(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
-                                pl.plane_b, Cd, pl.plane_c, engine == 2 ? 1 : 0, parts, raster, st));
+                                pl.plane_b, Cd, pl.plane_c, engine == 2 ? 1 : 0, parts, raster, st,
+                                pace));
   } else {
     MDG_TRY(launch_diag_gemm_v0(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
                                 pl.plane_b, Cd, pl.plane_c, st));

@@ -71,9 +71,12 @@ int launch_diag_gemm_v0(int s, int D, int Mp, int Np, int Kp, const void *dA, co
 // 128 x 256 tiles on one CTA, 0 uses CTA pairs when Mp % 256 == 0.  parts:
 // diagonal ranges per pair tile, 0 = chosen to fill the last wave.  raster:
 // pair tiles run across strips this many 256-column blocks wide (0 = auto).
+// pace: cross-cluster pacing window of the pair kernel in k-steps (0 = the
+// default, or MDG_TC_PACE when set; -1 = off).
 int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, const void *dB,
                         int ld, long long plane_a, long long plane_b, int *chunks,
-                        long long plane_c, int single, int parts, int raster, cudaStream_t st);
+                        long long plane_c, int single, int parts, int raster, cudaStream_t st,
+                        int pace = 0);
 // Renormalisation for P limbs with NW-word integers, V columns per thread
 // (instantiated in renorm_p{2,4,8,16}.cu).
 template <int P>
@@ -112,7 +115,7 @@ int tc_device_status();
 // 3 = tcgen05 CTA pairs
 int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *B, int ldb,
                    double *C, int ldc, void *ws, int engine, int parts, int raster,
-                   cudaStream_t st);
+                   cudaStream_t st, int pace = 0);
 
 // run_slice_gemm in two parts, for callers that split A into row panels
 // (the pipelined host path): slice_prepare_b computes the column exponents
@@ -121,7 +124,7 @@ int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *
 // and on all of B, so panels give the bits of one run_slice_gemm.
 int slice_prepare_b(const SlicePlan &pl, const double *B, int ldb, void *ws, cudaStream_t st);
 int slice_panel(const SlicePlan &pl, int rows, const double *A, int lda, double *C, int ldc,
-                void *ws, int engine, int parts, int raster, cudaStream_t st);
+                void *ws, int engine, int parts, int raster, cudaStream_t st, int pace = 0);
 
 // Which engine mdg_gemm uses for the BF16 form (MDG_SLICE_ENGINE=0/1 overrides).
 int default_engine();

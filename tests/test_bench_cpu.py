@@ -18,9 +18,14 @@ def test_cpu_baseline_legs_run_on_small_inputs(inputs, orc):
 
 def test_batched_tile_work_of_the_batched_workload(inputs):
     """Useful and padded BF16 work of the 256-problem batch (seed 3) at the
-    default digit counts 14 / 28 / 55."""
+    default digit counts 14 / 28 / 55: rows padded to 128, columns to the
+    tile policy's width, k to 16 (the last k-block issues only the MMAs
+    that reach data)."""
     bench = importlib.import_module("bench")
     probs, _ = inputs.batched_problems(256, seed=3)
     useful, padded = bench.batched_tile_work(probs, {2: 14, 4: 28, 8: 55})
-    assert abs(useful / 6.710e12 - 1) < 1e-3 and abs(padded / 1.168e13 - 1) < 1e-3
+    assert abs(useful / 6.710e12 - 1) < 1e-3 and abs(padded / 1.101e13 - 1) < 1e-3
+    _, padded128 = bench.batched_tile_work(probs, {2: 14, 4: 28, 8: 55}, "128")
+    _, padded_auto = bench.batched_tile_work(probs, {2: 14, 4: 28, 8: 55}, "auto")
+    assert padded_auto == padded128 < padded
     assert bench.batched_tile_work([(4, 128, 256, 64)], {4: 28}) == (2.0 * 128 * 256 * 64 * 406,) * 2

@@ -88,7 +88,8 @@ def test_workspace_sizes(L):
 
 
 @pytest.mark.parametrize("field,value", [("engine", 4), ("engine", -1), ("parts", 9), ("parts", -1),
-                                         ("raster", -1), ("split_exact", 3)])
+                                         ("raster", -1), ("split_exact", 3), ("pace", -2),
+                                         ("pace", 65537)])
 def test_bad_options_rejected(L, field, value):
     """Out-of-range mdg_options fields: no workspace size, and mdg_gemm
     returns MDG_ERROR_INVALID_FORM before touching the device."""
@@ -105,7 +106,7 @@ def test_schedule_options_accepted(L):
     api = pkg("api")
     base = api.workspace_size("slice_bf16", 4, 512, 512, 512)
     for kw in ({"engine": "tc_pair", "parts": 8, "raster": 1000}, {"engine": "mma_sync"},
-               {"engine": "tc", "parts": 1, "raster": 1}):
+               {"engine": "tc", "parts": 1, "raster": 1}, {"pace": -1}, {"pace": 128}):
         assert api.workspace_size("slice_bf16", 4, 512, 512, 512, **kw) == base
 
 

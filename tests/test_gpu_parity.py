@@ -315,6 +315,10 @@ def test_slice_gemm_schedules_bit_identical(api, inputs, monkeypatch):
         for parts, raster in ((0, 0), (1, 1), (3, 2), (2, 5), (8, 100)):
             got = host(api.gemm(A, B, "slice_bf16", engine="tc_pair", parts=parts, raster=raster))
             assert np.array_equal(got, ref), (pace, parts, raster)
+    monkeypatch.delenv("MDG_TC_PACE")
+    for pace_opt in (-1, 1, 32, 128):  # the pacing window as an option
+        got = host(api.gemm(A, B, "slice_bf16", engine="tc_pair", pace=pace_opt))
+        assert np.array_equal(got, ref), pace_opt
     assert api.device_status() == 0
 
 

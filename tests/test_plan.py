@@ -10,9 +10,10 @@ import pytest
 from conftest import pkg
 
 CACHE = {"NVIDIA GB300|13000": {"2 4 28 28 1024 1024 1024": {"engine": 2, "parts": 2,
-                                                            "raster": 8, "ms": 1.25},
+                                                            "raster": 8, "pace": 128,
+                                                            "ms": 1.25},
                                 "2 2 14 14 256 256 64": {"engine": 1, "parts": 0,
-                                                        "raster": 0, "ms": 0.01},
+                                                        "raster": 0, "pace": -1, "ms": 0.01},
                                 "batch 256 0123456789abcdef": {"tiles": 2, "ms": 13.5}},
          "other|1": {}}
 
@@ -44,7 +45,8 @@ def test_tune_cache_rejects_bad_files(tmp_path):
     for field, value in (("engine", "1e300"), ("engine", "-1"), ("engine", "4"),
                          ("engine", "nan"), ("parts", "9"), ("parts", "1.5"),
                          ("raster", "-1"), ("raster", "inf"), ("raster", "2e6"),
-                         ("tiles", "3"), ("tiles", "-1"), ("ms", "-1"), ("ms", "nan")):
+                         ("tiles", "3"), ("tiles", "-1"), ("pace", "-2"), ("pace", "70000"),
+                         ("ms", "-1"), ("ms", "nan")):
         bad.write_text('{"d": {"ok": {"engine": 2, "parts": 1}, '
                        f'"s": {{"{field}": {value}}}}}}}')
         assert L.mdg_tune_cache_load(str(bad).encode()) == 4, (field, value)
