@@ -489,7 +489,7 @@ class Plan:
     def schedule(self):
         o = Options()
         check(lib().mdg_plan_schedule(self.h, ctypes.byref(o)), "mdg_plan_schedule")
-        return {"engine": o.engine, "parts": o.parts, "raster": o.raster}
+        return {"engine": o.engine, "parts": o.parts, "raster": o.raster, "pace": o.pace}
 
     def close(self):
         if self.h:

@@ -27,7 +27,7 @@ import time
 
 from . import api, errors
 
-FORMS = ("plain", "fp64split", "slice_bf16")
+FORMS = ("plain", "fp64split", "slice_bf16", "fp64_digits")
 
 
 def _positive(text):
@@ -58,6 +58,8 @@ def build_parser():
         p.add_argument("--engine", default="auto", choices=sorted(api.ENGINES))
         p.add_argument("--parts", type=int, default=0, help="diagonal ranges per tile (0 = auto)")
         p.add_argument("--raster", type=int, default=0, help="tile strip width (0 = auto)")
+        p.add_argument("--pace", type=int, default=0,
+                       help="pacing window in k-steps (0 = default, -1 = off)")
 
     g = sub.add_parser("gemm", help="time one GEMM and report error bits")
     common(g)
@@ -77,7 +79,7 @@ def build_parser():
 def gemm_options(args):
     """The mdg_options fields the flags set (forwarded to api.gemm / api.Plan)."""
     return {"slices": args.slices, "diagonals": args.diagonals, "engine": args.engine,
-            "parts": args.parts, "raster": args.raster}
+            "parts": args.parts, "raster": args.raster, "pace": args.pace}
 
 
 def config(args):

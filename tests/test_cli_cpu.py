@@ -20,7 +20,7 @@ def test_flags_and_forwarded_options(cli):
     assert (a.cmd, a.p, a.m, a.n, a.k, a.form, a.iters, a.sample) == \
         ("gemm", 8, 64, 1024, 1024, "plain", 3, 3)
     assert cli.gemm_options(a) == {"slices": 0, "diagonals": 0, "engine": "tc_pair",
-                                   "parts": 2, "raster": 0}
+                                   "parts": 2, "raster": 0, "pace": 0}
     t = cli.build_parser().parse_args(["tune", "--cache", "x.json", "--slices", "30"])
     assert (t.cmd, t.cache, t.slices, t.p) == ("tune", "x.json", 30, 4)
     for bad in (["gemm", "--iters", "0"], ["gemm", "--p", "3"], ["gemm", "--form", "int8"], []):
