@@ -167,11 +167,17 @@ int mdg_batch_create(const mdg_problem *problems, int count, void *workspace,
 int mdg_batch_run(mdg_batch batch, void *stream);
 void mdg_batch_destroy(mdg_batch batch);
 
-/* Tile policies of the batched plan's diagonal GEMM: tiles of 128 rows by
- * 256 columns only, by 128 columns only, or (auto) 128 columns for the
- * problems where that pads fewer columns (n mod 256 in 1..128), else 256.
- * Every policy gives the same bits. */
-enum { MDG_BATCH_TILES_AUTO = 0, MDG_BATCH_TILES_256 = 1, MDG_BATCH_TILES_128 = 2 };
+/* Tile policies of the batched plan's diagonal GEMM: single-CTA tiles of
+ * 128 rows by 256 columns only, by 128 columns only, or (auto) 128 columns
+ * for the problems where that pads fewer columns (n mod 256 in 1..128), else
+ * 256; or CTA pairs with 256 x 256 tiles (half the operand bytes per
+ * product, rows padded to 256).  Every policy gives the same bits. */
+enum {
+  MDG_BATCH_TILES_AUTO = 0,
+  MDG_BATCH_TILES_256 = 1,
+  MDG_BATCH_TILES_128 = 2,
+  MDG_BATCH_TILES_PAIR = 3
+};
 /* Re-deals the plan's tiles under `policy` (uploads the tile table and
  * synchronises `stream`; not during a capture).  mdg_batch_tiles returns
  * the policy in use; a new plan starts with the policy recorded by

@@ -211,11 +211,11 @@ class BatchPlan:
         check(lib().mdg_batch_run(self.handle, _stream(stream)), "mdg_batch_run")
         return self.Cs
 
-    TILES = {"auto": 0, "256": 1, "128": 2}
+    TILES = {"auto": 0, "256": 1, "128": 2, "pair": 3}
 
     @property
     def tiles(self):
-        """The tile policy in use: "auto", "256" or "128"."""
+        """The tile policy in use: "auto", "256", "128" or "pair"."""
         code = lib().mdg_batch_tiles(self.handle)
         return {v: k for k, v in self.TILES.items()}[code]
 

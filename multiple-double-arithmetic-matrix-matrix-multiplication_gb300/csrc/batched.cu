@@ -45,16 +45,17 @@ namespace {
 
 using mdgi::BatchProblem;
 
-// Tile width of a problem's grouped-GEMM tiles under a policy: 256 columns
-// (the wider tile reads fewer operand bytes per product), or 128 where that
-// pads fewer columns (n mod 256 in 1..128), or 128 always.
+// Tile width of a problem's single-CTA grouped-GEMM tiles under a policy:
+// 256 columns (the wider tile reads fewer operand bytes per product), or 128
+// where that pads fewer columns (n mod 256 in 1..128), or 128 always.  The
+// CTA-pair policy uses 256 x 256 tiles.
 int tile_width(int policy, int n) {
   const int w128 = (int)mdgi::align_up(std::max(n, 1), 128);
   const int w256 = (int)mdgi::align_up(std::max(n, 1), 256);
   switch (policy) {
-    case MDG_BATCH_TILES_256: return 256;
     case MDG_BATCH_TILES_128: return 128;
-    default: return w128 < w256 ? 128 : 256;
+    case MDG_BATCH_TILES_AUTO: return w128 < w256 ? 128 : 256;
+    default: return 256;
   }
 }
 
@@ -63,13 +64,15 @@ int tile_width(int policy, int n) {
 int grouped_table(const std::vector<BatchProblem> &hp, int policy,
                   std::vector<mdgi::GroupedProblem> *hg, int *total_tiles) {
   hg->clear();
+  const bool pair = policy == MDG_BATCH_TILES_PAIR;
   for (const BatchProblem &b : hp) {
     mdgi::GroupedProblem g{};
     const int tn = tile_width(policy, b.n);
     MDG_TRY(mdgi::encode_plane_map(g.tmA, b.dA, b.Kp, (long long)b.s * b.Mp, 128));
-    MDG_TRY(mdgi::encode_plane_map(g.tmB, b.dB, b.Kp, (long long)b.s * b.Np, tn));
+    MDG_TRY(mdgi::encode_plane_map(g.tmB, b.dB, b.Kp, (long long)b.s * b.Np, pair ? 128 : tn));
     g.s = b.s; g.D = b.D; g.Mp = b.Mp; g.Np = b.Np; g.KB = b.Kp / 64;
     g.tn = tn;
+    g.mt = pair ? b.Mp / 256 : (b.m + 127) / 128;
     g.nt = (b.n + tn - 1) / tn;
     g.ktail = (b.k - (g.KB - 1) * 64 + 15) / 16;
     g.out = b.chunks;
@@ -94,7 +97,7 @@ int grouped_table(const std::vector<BatchProblem> &hp, int policy,
   int t = 0;
   for (mdgi::GroupedProblem &g : *hg) {
     g.tile_begin = t;
-    t += (g.Mp / 128) * g.nt;
+    t += g.mt * g.nt;
   }
   *total_tiles = t;
   return MDG_SUCCESS;
@@ -138,7 +141,8 @@ int plan_batch(const mdg_problem *problems, int count, Layout *L, mdg_batch_s *h
     const int i = order[oi];
     const mdg_problem &q = problems[i];
     const int s = mdg_default_slices(q.p), D = s;
-    const int Mp = (int)mdgi::align_up(std::max(q.m, 1), 128);
+    // rows padded to 256 so that every tile policy, CTA pairs included, fits
+    const int Mp = (int)mdgi::align_up(std::max(q.m, 1), 256);
     const int Np = (int)mdgi::align_up(std::max(q.n, 1), 256);
     const int Kp = (int)mdgi::align_up(std::max(q.k, 1), 64);
     const int nch = mdgi::total_chunks(s, D, Kp / 64);
@@ -303,7 +307,8 @@ int mdg_batch_run(mdg_batch_s *h, void *stream) {
     default: MDG_BATCH_STAGES(16); break;
   }
 #undef MDG_BATCH_STAGES
-  MDG_TRY(mdgi::launch_diag_gemm_grouped(h->dgroups, h->count, h->total_tiles, st));
+  MDG_TRY(mdgi::launch_diag_gemm_grouped(h->dgroups, h->count, h->total_tiles,
+                                         h->tiles_policy == MDG_BATCH_TILES_PAIR, st));
   const int *rb = h->renorm_begin, *rc = h->renorm_count, *rn = h->renorm_n;
   MDG_TRY(mdgi::launch_batch_renorm<2>(h->dprobs, h->count, rb[0], rc[0], rn[0], h->exps, st));
   MDG_TRY(mdgi::launch_batch_renorm<4>(h->dprobs, h->count, rb[1], rc[1], rn[1], h->exps, st));
@@ -314,7 +319,7 @@ int mdg_batch_run(mdg_batch_s *h, void *stream) {
 
 int mdg_batch_set_tiles(mdg_batch_s *h, int policy, void *stream) {
   if (!h) return MDG_ERROR_NULL_POINTER;
-  if (policy < MDG_BATCH_TILES_AUTO || policy > MDG_BATCH_TILES_128) return MDG_ERROR_INVALID_FORM;
+  if (policy < MDG_BATCH_TILES_AUTO || policy > MDG_BATCH_TILES_PAIR) return MDG_ERROR_INVALID_FORM;
   return apply_tiles(h, policy, mdgi::as_stream(stream));
 }
 
@@ -329,7 +334,8 @@ int mdg_batch_tune(mdg_batch_s *h, void *stream) {
   MDG_TRY_CUDA(cudaEventCreate(&e1));
   int best = h->tiles_policy, status = MDG_SUCCESS;
   float best_ms = 0.0f;
-  for (int policy : {MDG_BATCH_TILES_256, MDG_BATCH_TILES_AUTO, MDG_BATCH_TILES_128}) {
+  for (int policy : {MDG_BATCH_TILES_256, MDG_BATCH_TILES_AUTO, MDG_BATCH_TILES_128,
+                     MDG_BATCH_TILES_PAIR}) {
     status = apply_tiles(h, policy, st);
     if (status == MDG_SUCCESS) status = mdg_batch_run(h, stream);  // warm-up
     if (status != MDG_SUCCESS) break;

@@ -449,10 +449,10 @@ struct GroupedJobs {
       if (probs[mid].tile_begin <= t) lo = mid; else hi = mid - 1;
     }
     const mdgi::GroupedProblem &g = probs[lo];
-    const int lt = t - g.tile_begin, MB = g.Mp / TM;
+    const int lt = t - g.tile_begin;
     return TileJob{reinterpret_cast<const CUtensorMap *>(g.tmA),
                    reinterpret_cast<const CUtensorMap *>(g.tmB), g.s, g.D, g.Mp, g.Np, g.KB,
-                   (lt % MB) * TM, (lt / MB) * g.tn, g.tn, g.ktail, g.out, g.plane_c};
+                   (lt % g.mt) * TM, (lt / g.mt) * g.tn, g.tn, g.ktail, g.out, g.plane_c};
   }
 };
 
@@ -578,11 +578,77 @@ __device__ __forceinline__ uint32_t pace_load(int slot, int ncl, uint32_t epoch)
   return (uint32_t)(v >> 32) == epoch ? (uint32_t)v : 0u;
 }
 
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
-    diag_gemm_tc2_kernel(const __grid_constant__ CUtensorMap tmA,
-                         const __grid_constant__ CUtensorMap tmB, int s, int D, int Mp, int Np,
-                         int KB, int *__restrict__ out, long long plane_c, int parts,
-                         int raster, int pace, uint32_t epoch, int no_loads) {
+// One unit of work of the pair kernel: a 256 x 256 tile of one problem
+// (rows row0.., columns col0..) and the diagonals [d0, d1) it computes.
+struct PairJob {
+  const CUtensorMap *tmA, *tmB;
+  int s, D, Mp, Np, KB, row0, col0, d0, d1;
+  int *out;
+  long long plane_c;
+};
+
+// A single problem: units are tiles, or parts of tiles (ranges of
+// diagonals whose digit-pair counts add up to about 1/parts of the tile's
+// work), taken in strips of `raster` column blocks: tiles run across a strip
+// of `raster` column blocks, then down the rows, so that the clusters busy at
+// the same time read few distinct A row blocks and B column blocks and share
+// them in L2 (raster = 1 walks each column block top to bottom).
+struct PairSingle {
+  const CUtensorMap *tmA, *tmB;
+  int s, D, Mp, Np, KB;
+  int *out;
+  long long plane_c;
+  int parts, raster;
+  __device__ int units() const { return (Mp / 256) * (Np / TN2) * parts; }
+  __device__ PairJob job(int u) const {
+    const int MB = Mp / 256, NB = Np / TN2, tiles = MB * NB;
+    const int tile = u % tiles, part = u / tiles;
+    int total = 0;
+    for (int d = 0; d < D; ++d) total += mdgi::diag_pairs(d, s);
+    const long long lo = (long long)total * part / parts, hi = (long long)total * (part + 1) / parts;
+    int cum = 0, d0 = D, d1 = D;
+    for (int d = 0; d < D; ++d) {
+      if (cum >= lo && d0 == D) d0 = d;
+      if (cum >= hi) {
+        d1 = d;
+        break;
+      }
+      cum += mdgi::diag_pairs(d, s);
+    }
+    if (d0 > d1) d0 = d1;
+    const int strip = tile / (MB * raster);
+    const int idx = tile - strip * MB * raster;
+    const int c0 = strip * raster;
+    const int g = NB - c0 < raster ? NB - c0 : raster;
+    const int rb = idx / g, cb = c0 + idx - rb * g;
+    return PairJob{tmA, tmB, s, D, Mp, Np, KB, rb * 256, cb * TN2, d0, d1, out, plane_c};
+  }
+};
+
+// Many problems (GroupedProblem table in global memory, tensor maps with
+// 128-row boxes for A and B, Mp a multiple of 256): units are whole 256 x 256
+// tiles, numbered problem after problem (mt row tiles x nt column tiles each).
+struct PairGrouped {
+  const mdgi::GroupedProblem *probs;
+  int count, total;
+  __device__ int units() const { return total; }
+  __device__ PairJob job(int u) const {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (probs[mid].tile_begin <= u) lo = mid; else hi = mid - 1;
+    }
+    const mdgi::GroupedProblem &g = probs[lo];
+    const int lt = u - g.tile_begin;
+    return PairJob{reinterpret_cast<const CUtensorMap *>(g.tmA),
+                   reinterpret_cast<const CUtensorMap *>(g.tmB), g.s, g.D, g.Mp, g.Np, g.KB,
+                   (lt % g.mt) * 256, (lt / g.mt) * TN2, 0, g.D, g.out, g.plane_c};
+  }
+};
+
+template <class Jobs>
+__device__ __forceinline__ void tc2_body(const Jobs &jobs, int pace, uint32_t epoch,
+                                         int no_loads) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -634,46 +700,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
   fence_after();
   const uint32_t tmem_base = *tmem_holder;
 
-  const int MB = Mp / 256;
-  const int tiles = MB * (Np / TN2);
-  const int units = tiles * parts;
+  const int units = jobs.units();
   const int cid = blockIdx.x >> 1, ncl = gridDim.x >> 1;
   const bool pacer = leader && pace > 0 && ncl <= PACE_SLOTS;
-  // a unit is one part of one tile: the diagonals [d0, d1) whose digit-pair
-  // counts add up to about 1/parts of the tile's work
-  auto unit_range = [&](int u, int &tile, int &d0, int &d1) {
-    tile = u % tiles;
-    const int part = u / tiles;
-    int total = 0;
-    for (int d = 0; d < D; ++d) total += mdgi::diag_pairs(d, s);
-    const long long lo = (long long)total * part / parts, hi = (long long)total * (part + 1) / parts;
-    int cum = 0;
-    d0 = D;
-    d1 = D;
-    for (int d = 0; d < D; ++d) {
-      if (cum >= lo && d0 == D) d0 = d;
-      if (cum >= hi) {
-        d1 = d;
-        break;
-      }
-      cum += mdgi::diag_pairs(d, s);
-    }
-    if (d0 > d1) d0 = d1;
-  };
-  // tile -> (row block, column block).  Tiles run across a strip of
-  // `raster` column blocks, then down the rows, so that the clusters busy at
-  // the same time read few distinct A row blocks and B column blocks and
-  // share them in L2.  raster = 1 walks each column block top to bottom.
-  auto tile_rc = [&](int tile, int &rb, int &cb) {
-    const int NB = Np / TN2;
-    const int strip = tile / (MB * raster);
-    const int idx = tile - strip * MB * raster;
-    const int c0 = strip * raster;
-    const int g = NB - c0 < raster ? NB - c0 : raster;
-    rb = idx / g;
-    cb = c0 + idx - rb * g;
-  };
-
   if (warp == 0) {
     if (lane == 0) {
       // ------------------------------------------------------ producer --
@@ -688,13 +717,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
       // MMA thread's wait for data runs out, it raises the abort flag and
       // every role leaves with nothing in flight
       for (int u = no_loads ? units : cid; u < units; u += ncl) {
-        int tile, d0, d1;
-        unit_range(u, tile, d0, d1);
-        int rb, cb;
-        tile_rc(tile, rb, cb);
-        const int row = rb * 256 + (int)rank * TM;
-        const int col = cb * TN2 + (int)rank * BH;
-        for (int d = d0; d < d1; ++d) {
+        const PairJob jb = jobs.job(u);
+        const int s = jb.s, KB = jb.KB;
+        const int row = jb.row0 + (int)rank * TM;
+        const int col = jb.col0 + (int)rank * BH;
+        for (int d = jb.d0; d < jb.d1; ++d) {
           const int ilo = d - (s - 1) > 0 ? d - (s - 1) : 0;
           const int S = mdgi::diag_pairs(d, s) * KB;
           for (int t = 0; t < S; ++t) {
@@ -713,8 +740,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
             if (leader) mbar_expect_tx(full(st), 2 * STAGE2_BYTES);
             const uint32_t a_dst = smem_base + st * STAGE2_BYTES;
             const uint32_t bar0 = map_to_rank0(full(st));
-            tma_load_2d_pair(a_dst, &tmA, kb * TK, i * Mp + row, bar0);
-            tma_load_2d_pair(a_dst + A2_BYTES, &tmB, kb * TK, j * Np + col, bar0);
+            tma_load_2d_pair(a_dst, jb.tmA, kb * TK, i * jb.Mp + row, bar0);
+            tma_load_2d_pair(a_dst + A2_BYTES, jb.tmB, kb * TK, j * jb.Np + col, bar0);
             last_par = (last_par & ~(1u << st)) | (ph << st);
             issued |= 1u << st;
             if (++st == STAGES2) {
@@ -738,10 +765,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
       uint32_t ph = 0, aph[2] = {0, 0};
       bool any = false;
       for (int u = cid; u < units; u += ncl) {
-        int tile, d0, d1;
-        unit_range(u, tile, d0, d1);
-        for (int d = d0; d < d1; ++d) {
-          const int S = mdgi::diag_pairs(d, s) * KB;
+        const PairJob jb = jobs.job(u);
+        for (int d = jb.d0; d < jb.d1; ++d) {
+          const int S = mdgi::diag_pairs(d, jb.s) * jb.KB;
           for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
             if (!mbar_wait(accempty(buf), aph[buf] ^ 1, abort_flag)) goto mma_done;
             fence_after();
@@ -817,16 +843,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
     uint32_t aph[2] = {0, 0};
     const uint32_t accempty0[2] = {map_to_rank0(accempty(0)), map_to_rank0(accempty(1))};
     for (int u = cid; u < units; u += ncl) {
-      int tile, d0, d1;
-      unit_range(u, tile, d0, d1);
-      int rb, cb;
-      tile_rc(tile, rb, cb);
-      const int row = rb * 256 + (int)rank * TM + 32 * q + lane;
-      const int col = cb * TN2 + 128 * h;
+      const PairJob jb = jobs.job(u);
+      const int row = jb.row0 + (int)rank * TM + 32 * q + lane;
+      const int col = jb.col0 + 128 * h;
       int chunk = 0;
-      for (int d = 0; d < d0; ++d) chunk += mdgi::diag_chunks(d, s, KB);
-      for (int d = d0; d < d1; ++d) {
-        const int S = mdgi::diag_pairs(d, s) * KB;
+      for (int d = 0; d < jb.d0; ++d) chunk += mdgi::diag_chunks(d, jb.s, jb.KB);
+      for (int d = jb.d0; d < jb.d1; ++d) {
+        const int S = mdgi::diag_pairs(d, jb.s) * jb.KB;
         for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
           int ok = 1;
           if (lane == 0) ok = mbar_wait(accfull(buf), aph[buf], abort_flag) ? 1 : 0;
@@ -842,8 +865,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
           buf ^= 1;
           const int g1 = g0 + mdgi::GROUP_STEPS;
           if (g1 % mdgi::CHUNK_STEPS == 0 || g1 >= S) {
-            int4 *dst = reinterpret_cast<int4 *>(out + (size_t)chunk * plane_c +
-                                                 (size_t)row * Np + col);
+            int4 *dst = reinterpret_cast<int4 *>(jb.out + (size_t)chunk * jb.plane_c +
+                                                 (size_t)row * jb.Np + col);
 #pragma unroll
             for (int v = 0; v < 32; ++v) {
               dst[v] = make_int4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
@@ -865,6 +888,23 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
                  "r"(TMEM_COLS)
                  : "memory");
   if (threadIdx.x == 0 && *abort_flag) atomicExch(&g_tc_error, 1);
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
+    diag_gemm_tc2_kernel(const __grid_constant__ CUtensorMap tmA,
+                         const __grid_constant__ CUtensorMap tmB, int s, int D, int Mp, int Np,
+                         int KB, int *__restrict__ out, long long plane_c, int parts,
+                         int raster, int pace, uint32_t epoch, int no_loads) {
+  tc2_body(PairSingle{&tmA, &tmB, s, D, Mp, Np, KB, out, plane_c, parts, raster}, pace, epoch,
+           no_loads);
+}
+
+// The batched plan's grouped GEMM on CTA pairs (no pacing: the clusters work
+// on different problems).
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS2, 1)
+    diag_gemm_tc2_grouped_kernel(const mdgi::GroupedProblem *__restrict__ probs, int count,
+                                 int total) {
+  tc2_body(PairGrouped{probs, count, total}, 0, 0, 0);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -988,15 +1028,25 @@ int encode_plane_map(void *map128, const void *base, int Kp, long long rows_tota
 }
 
 int launch_diag_gemm_grouped(const GroupedProblem *dev_probs, int count, int total_tiles,
-                             cudaStream_t st) {
+                             int pair, cudaStream_t st) {
   if (total_tiles == 0) return MDG_SUCCESS;
   int dev = 0, sms = 0;
   MDG_TRY_CUDA(cudaGetDevice(&dev));
-  MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc_grouped_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
   MDG_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int grid = total_tiles < sms ? total_tiles : sms;
-  diag_gemm_tc_grouped_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(dev_probs, count, total_tiles);
+  if (pair) {
+    MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc2_grouped_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
+    const int ncl = sms / 2;
+    const int clusters = total_tiles < ncl ? total_tiles : ncl;
+    diag_gemm_tc2_grouped_kernel<<<2 * clusters, THREADS2, SMEM2_BYTES, st>>>(dev_probs, count,
+                                                                            total_tiles);
+  } else {
+    MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc_grouped_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    const int grid = total_tiles < sms ? total_tiles : sms;
+    diag_gemm_tc_grouped_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(dev_probs, count,
+                                                                   total_tiles);
+  }
   MDG_TRY_LAUNCH();
   return MDG_SUCCESS;
 }

@@ -315,7 +315,7 @@ int mdg_tune_cache_load(const char *path) {
         if (field == "parts") return whole_in(v, 0, 8, &e.parts);
         if (field == "raster") return whole_in(v, 0, 1 << 20, &e.raster);
         if (field == "pace") return whole_in(v, -1, 65536, &e.pace);
-        if (field == "tiles") return whole_in(v, 0, 2, &e.tiles);
+        if (field == "tiles") return whole_in(v, 0, 3, &e.tiles);
         if (field == "ms") {
           if (!(v >= 0.0 && v <= 1e12)) return false;
           e.ms = v;

@@ -86,15 +86,17 @@ int launch_renorm_p(int NW, int V, int s, int D, int KB, int m, int n, const int
 int launch_renorm(int p, int s, int D, int KB, int m, int n, const int *chunks,
                   long long plane_c, int ldcd, const int *E, const int *F, double *C, int ldc,
                   cudaStream_t st);
-// One problem of a grouped diagonal GEMM (single-CTA tcgen05 kernel,
-// tiles of 128 rows x tn columns, tn = 256 or 128): tensor maps of its digit
-// planes, sizes, first global tile, column tiles nt, output chunk planes.
-// ktail: MMAs of K = 16 that reach data in the last 64-deep k-block (1..4).
-// Lives in global memory, 64-byte aligned.
+// One problem of a grouped diagonal GEMM: the single-CTA tcgen05 kernel
+// (tiles of 128 rows x tn columns, tn = 256 or 128) or the CTA-pair kernel
+// (tiles of 256 x 256; B box of 128 rows, one half per CTA).  Tensor maps of
+// its digit planes, sizes, first global tile, row tiles mt and column tiles
+// nt, output chunk planes.  ktail: MMAs of K = 16 that reach data in the last
+// 64-deep k-block (1..4; single-CTA kernel).  Lives in global memory,
+// 64-byte aligned.
 struct alignas(64) GroupedProblem {
   unsigned char tmA[128];  // CUtensorMap, A planes, box 64 x 128
-  unsigned char tmB[128];  // CUtensorMap, B planes, box 64 x tn
-  int s, D, Mp, Np, KB, tile_begin, tn, nt, ktail;
+  unsigned char tmB[128];  // CUtensorMap, B planes, box 64 x tn (pairs: 64 x 128)
+  int s, D, Mp, Np, KB, tile_begin, tn, mt, nt, ktail;
   int *out;
   long long plane_c;
 };
@@ -104,8 +106,9 @@ int encode_plane_map(void *map128, const void *base, int Kp, long long rows_tota
 // (*policy is left alone otherwise), and a new record.
 void tune_lookup_batch(const std::string &key, int *policy);
 void tune_record_batch(const std::string &key, int policy, double ms);
+// pair: the CTA-pair kernel (Mp of every problem a multiple of 256).
 int launch_diag_gemm_grouped(const GroupedProblem *dev_probs, int count, int total_tiles,
-                             cudaStream_t st);
+                             int pair, cudaStream_t st);
 
 // Waits for the device; MDG_ERROR_TIMEOUT if a bounded wait of the tcgen05
 // engine gave up since the last call (the flag is then cleared).

@@ -553,7 +553,8 @@ def test_batched_plan_graph_capture(api, orc, inputs):
 
 def test_batched_tile_policies_bit_identical_and_tuned(api, orc, inputs):
     """The grouped GEMM under each tile policy (256-column tiles, 128-column
-    tiles, and the per-problem choice) over problems whose n falls on both
+    tiles, the per-problem choice, and 256 x 256 tiles on CTA pairs) over
+    problems whose n falls on both
     sides of a 256 boundary and whose k ends inside a 64-deep block (the
     last block issues fewer MMAs): every problem's C equals the
     single-problem GEMM under every policy; tuning keeps one of them and
@@ -566,7 +567,7 @@ def test_batched_tile_policies_bit_identical_and_tuned(api, orc, inputs):
     want = [api.gemm(A, B, "slice_bf16") for A, B in ops]
     plan = api.BatchPlan(ops)
     assert plan.tiles == "256"
-    for policy in ("auto", "128", "256"):
+    for policy in ("auto", "128", "pair", "256"):
         plan.set_tiles(policy)
         for C in plan.Cs:
             C.fill_(np.nan)
@@ -576,7 +577,7 @@ def test_batched_tile_policies_bit_identical_and_tuned(api, orc, inputs):
             assert torch.equal(C, W), (policy, probs[i])
     api.tune_cache_clear()
     best = plan.tune()
-    assert best in ("auto", "256", "128")
+    assert best in ("auto", "256", "128", "pair")
     assert api.tune_cache_size() == 1
     again = api.BatchPlan(ops)  # same shapes: starts with the tuned policy
     assert again.tiles == best

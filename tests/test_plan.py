@@ -45,7 +45,7 @@ def test_tune_cache_rejects_bad_files(tmp_path):
     for field, value in (("engine", "1e300"), ("engine", "-1"), ("engine", "4"),
                          ("engine", "nan"), ("parts", "9"), ("parts", "1.5"),
                          ("raster", "-1"), ("raster", "inf"), ("raster", "2e6"),
-                         ("tiles", "3"), ("tiles", "-1"), ("pace", "-2"), ("pace", "70000"),
+                         ("tiles", "4"), ("tiles", "-1"), ("pace", "-2"), ("pace", "70000"),
                          ("ms", "-1"), ("ms", "nan")):
         bad.write_text('{"d": {"ok": {"engine": 2, "parts": 1}, '
                        f'"s": {{"{field}": {value}}}}}}}')
