@@ -446,8 +446,12 @@ def bench_form_line(api, ex, stream, P, A, B, form, dA, dB, sample, iters=1, row
     out = torch.empty((m, n, P), dtype=torch.float64, device="cuda")
     w = torch.empty(max(1, api.workspace_size(form, P, m, n, k)), dtype=torch.uint8,
                     device="cuda")
-    api.gemm(dA, dB, form, out=out, workspace=w)
-    t = event_time(lambda: api.gemm(dA, dB, form, out=out, workspace=w), stream, iters=iters)
+    # the first call is timed too: a form that takes seconds is measured on it
+    # (loading its kernels is a negligible part), a fast one on `iters` more
+    t = event_time(lambda: api.gemm(dA, dB, form, out=out, workspace=w), stream, iters=1)
+    if t < 1.0:
+        t = event_time(lambda: api.gemm(dA, dB, form, out=out, workspace=w), stream,
+                       iters=iters)
     r = [i for i in sample[0] if i < m]
     eb = ex.error_bits(out.cpu().numpy(), A, B, r, sample[1])
     del out, w
