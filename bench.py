@@ -486,6 +486,16 @@ def bench_forms(api, inputs, ex, stream):
         block = {}
         block["slice_bf16"] = bench_form_line(api, ex, stream, P, A, B, "slice_bf16", dA, dB,
                                               sample, iters=3)
+        # the same GEMM through a tuned plan (mdg_plan_tune: engines, parts, tile
+        # strips and pacing windows that give the same bits)
+        plan = api.Plan("slice_bf16", P, m, n, k)
+        Ct = torch.empty((m, n, P), dtype=torch.float64, device="cuda")
+        plan.tune(dA, dB, Ct)
+        tt = event_time(lambda: plan.run(dA, dB, Ct), stream, iters=3)
+        block["slice_bf16_tuned"] = {"gflops": 2.0 * m * n * k / tt / 1e9, "ms": tt * 1e3,
+                                     "schedule": plan.schedule()}
+        plan.close()
+        del Ct
         block["fp64split"] = bench_form_line(api, ex, stream, P, A, B, "fp64split", dA, dB,
                                              sample)
         block["fp64_digits"] = bench_form_line(api, ex, stream, P, A, B, "fp64_digits", dA, dB,
