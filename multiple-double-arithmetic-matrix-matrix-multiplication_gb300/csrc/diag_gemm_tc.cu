@@ -998,7 +998,11 @@ int launch_diag_gemm_tc(int s, int D, int Mp, int Np, int Kp, const void *dA, co
     // pacing window in k-steps, 0 = off (MDG_TC_PACE overrides); every
     // launch gets its own epoch so that slots left by earlier launches read
     // as "not started"
-    int pace = kDefaultPace;
+    // With no more units than clusters every tile is in work at once and
+    // the operands of the whole GEMM are read in one sweep: pacing has no
+    // drift to correct there and only costs (qd 1024^3: 7 % slower paced), so
+    // the default turns it off; an explicit window still applies.
+    int pace = units <= ncl ? 0 : kDefaultPace;
     if (const char *e = std::getenv("MDG_TC_PACE")) pace = std::max(0, std::atoi(e));
     if (pace_opt > 0) pace = pace_opt;
     if (pace_opt < 0) pace = 0;
