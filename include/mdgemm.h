@@ -150,6 +150,14 @@ int mdg_gemm_batched(int form, const mdg_problem *problems, int count,
 
 void mdg_release_cache(void);
 
+/* Page-locked host memory for the buffers of mdg_gemm_host (cudaHostAlloc,
+ * portable to every device): copies from it run at the host link's full
+ * rate, without the staging a pageable buffer needs.  *out is NULL on a
+ * failure (MDG_ERROR_ALLOCATION).  Not in the reference, whose wrappers copy
+ * from pageable std::vector storage. */
+int mdg_host_alloc(size_t bytes, void **out);
+void mdg_host_free(void *ptr);
+
 /* Batched BF16 slice-digit GEMM as a reusable plan.  mdg_batch_create lays
  * out `workspace` (mdg_batch_workspace_size bytes) for these problems
  * (device pointers, P in {2,4,8,16}, m, n, k >= 1, default digits per P),

@@ -45,6 +45,8 @@ SIGNATURES = {
     "mdg_gemm_batched_workspace_size": (c_size, [c_int, _P_PROB, c_int, _P_OPT]),
     "mdg_gemm_batched": (c_int, [c_int, _P_PROB, c_int, _P_OPT, c_vp, c_size, c_vp]),
     "mdg_release_cache": (None, []),
+    "mdg_host_alloc": (c_int, [c_size, ctypes.POINTER(c_vp)]),
+    "mdg_host_free": (None, [c_vp]),
     "mdg_split": (c_int, [c_int, c_int, c_int, c_ll, c_vp, c_vp, c_vp]),
     "mdg_split_planes": (c_int, [c_int, c_int, c_int, c_ll, c_vp, c_vp, c_ll, c_vp]),
     "mdg_plane_conv": (c_int, [c_int] * 4 + [c_vp, c_vp, c_vp, c_vp]),

@@ -164,6 +164,29 @@ def gemm_host(A, B, form="slice_bf16", **kw):
     return C
 
 
+class HostBuffer:
+    """Page-locked host memory from mdg_host_alloc, seen as a numpy array
+    (and, through torch.from_numpy, a CPU tensor) of `shape` float64: the
+    buffers mdg_gemm_host copies from and to at the host link's full rate."""
+
+    def __init__(self, shape):
+        self.shape = tuple(int(v) for v in shape)
+        count = int(np.prod(self.shape)) if self.shape else 1
+        p = ctypes.c_void_p()
+        check(lib().mdg_host_alloc(8 * count, ctypes.byref(p)), "mdg_host_alloc")
+        self.ptr = p
+        buf = (ctypes.c_double * count).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=np.float64, count=count).reshape(self.shape)
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self.array = None
+            lib().mdg_host_free(self.ptr)
+            self.ptr = None
+
+    __del__ = close
+
+
 def gemm_batched(problems, form="plain", stream=None, **kw):
     """problems: list of (A, B) device tensor pairs; returns the list of C."""
     Cs, table, keep = [], (Problem * len(problems))(), []

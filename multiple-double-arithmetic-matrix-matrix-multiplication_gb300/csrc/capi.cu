@@ -408,6 +408,23 @@ int mdg_gemm_host(int form, int p, int m, int n, int k, const double *A, const d
 
 void mdg_release_cache(void) { g_cache.release(); }
 
+int mdg_host_alloc(size_t bytes, void **out) {
+  if (!out) return MDG_ERROR_NULL_POINTER;
+  *out = nullptr;
+  if (alloc_over_limit(bytes)) return MDG_ERROR_ALLOCATION;
+  cudaError_t e = cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocPortable);
+  if (e != cudaSuccess) {
+    set_cuda_error(e);
+    *out = nullptr;
+    return MDG_ERROR_ALLOCATION;
+  }
+  return MDG_SUCCESS;
+}
+
+void mdg_host_free(void *ptr) {
+  if (ptr) cudaFreeHost(ptr);
+}
+
 // ---------------------------------------------------------------- batched --
 
 size_t mdg_gemm_batched_workspace_size(int form, const mdg_problem *problems, int count,
