@@ -435,6 +435,29 @@ def test_host_entry_matches_device_entry(api, inputs):
         assert np.array_equal(dC, hC), form
 
 
+def test_host_entry_with_library_pinned_buffers(api, inputs):
+    """mdg_gemm_host on page-locked buffers from mdg_host_alloc (api.HostBuffer),
+    the pipelined panel path included (m >= 2048): same bits as the device
+    entry; the buffers are freed and allocated again without leaking."""
+    import ctypes
+    _lib = pkg("_lib")
+    L = _lib.lib()
+    P, A, B = inputs.workload("qd1024", 2100, 90, 60)
+    m, k = A.shape[:2]
+    n = B.shape[1]
+    want = host(api.gemm(dev(A), dev(B), "slice_bf16"))
+    for _ in range(2):
+        hA, hB, hC = api.HostBuffer(A.shape), api.HostBuffer(B.shape), api.HostBuffer((m, n, P))
+        hA.array[...] = A
+        hB.array[...] = B
+        hC.array[...] = np.nan
+        _lib.check(L.mdg_gemm_host(2, P, m, n, k, hA.ptr, hB.ptr, hC.ptr, None), "host")
+        assert np.array_equal(hC.array, want)
+        for b in (hA, hB, hC):
+            b.close()
+    assert L.mdg_host_alloc(8, None) == 3
+
+
 @pytest.mark.parametrize("m,n,k", [(2600, 300, 200), (4500, 130, 70)])
 def test_pipelined_host_entry_matches_device_entry(api, inputs, m, n, k):
     """mdg_gemm_host of the BF16 form on m >= 2048 rows copies A in row
