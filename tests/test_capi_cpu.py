@@ -112,8 +112,8 @@ def test_schedule_options_accepted(L):
 
 def test_allocation_cap_simulates_out_of_memory(L, monkeypatch):
     """Host-side fault injection: MDG_ALLOC_LIMIT_BYTES makes the library's
-    own device allocations (the host entry's buffers, plan workspaces) fail
-    with MDG_ERROR_ALLOCATION before any CUDA call."""
+    own allocations (the host entry's buffers, plan workspaces, page-locked
+    host buffers) fail with MDG_ERROR_ALLOCATION before any CUDA call."""
     import numpy as np
     monkeypatch.setenv("MDG_ALLOC_LIMIT_BYTES", "1024")
     A = np.zeros((64, 64, 4))
@@ -123,6 +123,10 @@ def test_allocation_cap_simulates_out_of_memory(L, monkeypatch):
         assert L.mdg_gemm_host(form, 4, 64, 64, 64, ptr(A), ptr(A), ptr(C), None) == 9
     h = ctypes.c_void_p()
     assert L.mdg_plan_create(2, 4, 64, 64, 64, None, ctypes.byref(h)) == 9
+    # page-locked host buffers count too
+    p = ctypes.c_void_p(1)
+    assert L.mdg_host_alloc(4096, ctypes.byref(p)) == 9 and p.value is None
+    assert L.mdg_host_alloc(8, None) == 3
     assert L.mdg_status_string(9) == b"allocation failed"
 
 
