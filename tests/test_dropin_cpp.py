@@ -226,7 +226,7 @@ def test_gpu_exported_plain_kernels_match_reference(prog, tmp_path, P, name):
 @pytest.mark.parametrize("P", [2, 4, 8])
 def test_gpu_matmulTC_wrapper_all_forms(prog, tmp_path, orc, inputs, P):
     """matmulTC in the plain (bit for bit), FP64-split (oracle error bits
-    within 2) and BF16 slice (bit for bit vs the oracle) forms."""
+    within 2), BF16 slice and FP64 digit (bit for bit vs the oracle) forms."""
     ex = pkg("errors")
     n = 24
     rng = np.random.default_rng(P + 40)
@@ -237,6 +237,9 @@ def test_gpu_matmulTC_wrapper_all_forms(prog, tmp_path, orc, inputs, P):
     s = pkg("api").default_slices(P)
     sl = _roundtrip(prog, tmp_path, ["tc", 2, P, n], [A, B], (n, n, P))
     assert np.array_equal(sl, orc.gemm_slices(P, s, s, A, B, n, n, n))
+    s19 = pkg("api").default_slices(P, "fp64_digits")
+    fd = _roundtrip(prog, tmp_path, ["tc", 3, P, n], [A, B], (n, n, P))
+    assert np.array_equal(fd, orc.gemm_digits(P, s19, s19, A, B, n, n, n))
     sp = _roundtrip(prog, tmp_path, ["tc", 1, P, n], [A, B], (n, n, P))
     ref = orc.gemm_fp64split(P, A, B, n, n, n)
     bits = ex.error_bits(sp, A, B, range(n), range(n))
