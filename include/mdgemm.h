@@ -77,7 +77,8 @@ typedef struct {
   int raster;       /* BF16 form, CTA pairs: tile order runs across strips this many
                        256-column blocks wide (0: auto) */
   int pace;         /* BF16 form, CTA pairs: cross-cluster pacing window in k-steps
-                       (0: default 64, or MDG_TC_PACE when set; -1: off; at most 65536) */
+                       (0: default 64, off when every tile runs in the first wave of
+                       clusters, or MDG_TC_PACE when set; -1: off; at most 65536) */
 } mdg_options;
 
 /* One problem of a batched call. */
