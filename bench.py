@@ -357,7 +357,7 @@ def bench_batched(api, inputs, stream):
     def captured(pairs, tune=False):
         plan = api.BatchPlan(pairs)
         if tune:
-            plan.tune()  # tile policy: times 256-, auto- and 128-column tiles
+            plan.tune()  # times every tile policy and split mode, keeps the fastest
         plan.run()
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
@@ -410,13 +410,16 @@ def bench_batched(api, inputs, stream):
             # renormalisation per limb count present
             "slice_launches_per_batch": 3 + len({pr[0] for pr in probs}),
             "tile_policy": policy,
+            "split": plan.split,
             "plain_loop_gflops": flops / t_loop / 1e9, "plain_loop_ms": t_loop * 1e3,
             "plain_batched_gflops": flops / t_pb / 1e9, "plain_batched_ms": t_pb * 1e3,
             "slice_equals_single_problem": bool(same),
             "diag_bf16_tflop": {"useful": useful / 1e12, "padded": padded / 1e12,
                                 "useful_frac": useful / padded,
-                                "tiles": f"128 x {policy} columns (tuned policy), k padded to "
-                                         "16 (grouped single-CTA kernel)"}}
+                                "tiles": ("256 x 256 (CTA pairs, rows padded to 256)"
+                                          if policy == "pair" else
+                                          f"128 x {policy} columns (single CTA)")
+                                         + " under the tuned policy, k padded to 16"}}
 
 
 # FP64 operations per multi-double multiply-add of the plain form, the

@@ -51,8 +51,9 @@ enum {
   MDG_FORM_FP64_SPLIT = 1,
   /* Slice digits on BF16 tensor cores: exact 8-bit balanced digits per
    * operand with a shared exponent per row of A / column of B, exact
-   * diagonal sums (FP32 accumulation flushed every 256 products into
-   * integers), exact rounding back to P limbs.  No reference counterpart:
+   * diagonal sums (FP32 accumulation flushed into integers before a partial
+   * sum can pass 2^24: every 1024 products on tcgen05, every 256 on the
+   * mma.sync engine), exact rounding back to P limbs.  No reference counterpart:
    * this is the tensor-core form the reference set out to build. */
   MDG_FORM_SLICE_BF16 = 2,
   /* The same slice-digit scheme on the FP64 tensor cores the reference
@@ -193,10 +194,18 @@ enum {
  * mdg_batch_tune for its problem shapes, else MDG_BATCH_TILES_256. */
 int mdg_batch_set_tiles(mdg_batch batch, int policy, void *stream);
 int mdg_batch_tiles(mdg_batch batch);
-/* Times one mdg_batch_run under each tile policy (after a warm-up each),
- * keeps the fastest and records it in the tuning cache under the batch's
- * problem shapes; mdg_batch_create starts later plans of the same shapes
- * with the recorded policy.  Synchronises `stream`. */
+/* Split mode of the diagonal GEMM's work: 0 = each tile is one unit; 1 =
+ * heavy tiles are cut into ranges of diagonals, so that units carry about
+ * equal work and the units of one problem run side by side on the GPU
+ * (its digit planes then stay in L2 while they are reused).  Same bits
+ * either way; uploads the table and synchronises `stream` like
+ * mdg_batch_set_tiles.  mdg_batch_split returns the mode in use. */
+int mdg_batch_set_split(mdg_batch batch, int split, void *stream);
+int mdg_batch_split(mdg_batch batch);
+/* Times one mdg_batch_run under each tile policy and split mode (after a
+ * warm-up each), keeps the fastest and records it in the tuning cache under
+ * the batch's problem shapes; mdg_batch_create starts later plans of the
+ * same shapes with the recorded choice.  Synchronises `stream`. */
 int mdg_batch_tune(mdg_batch batch, void *stream);
 
 /* C = A * B in the BF16 slice-digit form (default digits) without any

@@ -78,6 +78,8 @@ SIGNATURES = {
     "mdg_batch_destroy": (None, [c_vp]),
     "mdg_batch_set_tiles": (c_int, [c_vp, c_int, c_vp]),
     "mdg_batch_tiles": (c_int, [c_vp]),
+    "mdg_batch_set_split": (c_int, [c_vp, c_int, c_vp]),
+    "mdg_batch_split": (c_int, [c_vp]),
     "mdg_batch_tune": (c_int, [c_vp, c_vp]),
     "mdg_gemm_slice_static": (c_int, [c_int] * 4 + [c_vp, c_int, c_vp, c_int, c_vp, c_int, c_vp]),
 }

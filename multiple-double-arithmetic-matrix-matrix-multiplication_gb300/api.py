@@ -247,9 +247,21 @@ class BatchPlan:
         check(lib().mdg_batch_set_tiles(self.handle, self.TILES[str(policy)], _stream(stream)),
               "mdg_batch_set_tiles")
 
+    @property
+    def split(self):
+        """True when heavy tiles are cut into diagonal ranges (the default)."""
+        return bool(lib().mdg_batch_split(self.handle))
+
+    def set_split(self, split, stream=None):
+        """Cut heavy tiles into diagonal ranges (True) or keep whole tiles
+        (False); same bits either way."""
+        check(lib().mdg_batch_set_split(self.handle, 1 if split else 0, _stream(stream)),
+              "mdg_batch_set_split")
+
     def tune(self, stream=None):
-        """Time every tile policy on the plan's operands, keep the fastest
-        (recorded in the tuning cache for plans of the same shapes)."""
+        """Time every tile policy and split mode on the plan's operands, keep
+        the fastest (recorded in the tuning cache for plans of the same
+        shapes); returns the tile policy."""
         check(lib().mdg_batch_tune(self.handle, _stream(stream)), "mdg_batch_tune")
         return self.tiles
 

@@ -13,9 +13,10 @@
 // Each stage kernel finds its problem from its block index by binary search
 // over per-problem prefix counts, and branches on the problem's P to the
 // integer width that P needs (batched_stages.cuh).  The grouped GEMM's tiles
-// are 128 rows by 256 or 128 columns per problem (a tile policy the plan
-// can tune).  Each problem's result equals the single-problem mdg_gemm
-// result bit for bit.  The reference runs one square problem per call; it
+// are 128 rows by 256 or 128 columns per problem, or 256 x 256 on CTA pairs
+// (a tile policy the plan can tune); heavy tiles can be cut into ranges of
+// diagonals (the split mode, tuned too).  Each problem's result equals the
+// single-problem mdg_gemm result bit for bit.  The reference runs one square problem per call; it
 // has no counterpart of this entry.
 #include <algorithm>
 #include <cstdio>
@@ -30,11 +31,11 @@
 #include "batched_table.cuh"
 
 struct mdg_batch_s {
-  int count = 0, nwmax = 4, total_tiles = 0;
+  int count = 0, nwmax = 4, total_units = 0;
   int scale_units = 0, digit_units = 0, renorm_units = 0;
   // per P = 2, 4, 8, 16: first output row, rows, widest n
   int renorm_begin[4] = {0, 0, 0, 0}, renorm_count[4] = {0, 0, 0, 0}, renorm_n[4] = {0, 0, 0, 0};
-  int tiles_policy = MDG_BATCH_TILES_256;
+  int tiles_policy = MDG_BATCH_TILES_256, split = 1;
   mdgi::BatchProblem *dprobs = nullptr;
   mdgi::GroupedProblem *dgroups = nullptr;
   int *exps = nullptr;  // E of all problems then F
@@ -59,10 +60,17 @@ int tile_width(int policy, int n) {
   }
 }
 
-// The grouped GEMM's table for a tile policy: B tensor maps with the
-// policy's box, tiles dealt heaviest first.
-int grouped_table(const std::vector<BatchProblem> &hp, int policy,
-                  std::vector<mdgi::GroupedProblem> *hg, int *total_tiles) {
+// Work units per worker (CTA, or CTA pair) that the split mode aims for:
+// heavy tiles are cut into diagonal ranges of about total / (workers x this)
+// k-steps of work.  Small units keep the units of one problem side by side
+// on the GPU, so that its digit planes are read from DRAM about once rather
+// than once per digit pair.
+constexpr int kSplitUnitsPerWorker = 16;
+
+// The grouped GEMM's table for a tile policy and split mode: B tensor maps
+// with the policy's box, units dealt heaviest first.
+int grouped_table(const std::vector<BatchProblem> &hp, int policy, int split, int workers,
+                  std::vector<mdgi::GroupedProblem> *hg, int *total_units) {
   hg->clear();
   const bool pair = policy == MDG_BATCH_TILES_PAIR;
   for (const BatchProblem &b : hp) {
@@ -75,31 +83,46 @@ int grouped_table(const std::vector<BatchProblem> &hp, int policy,
     g.mt = pair ? b.Mp / 256 : (b.m + 127) / 128;
     g.nt = (b.n + tn - 1) / tn;
     g.ktail = (b.k - (g.KB - 1) * 64 + 15) / 16;
+    g.parts = 1;
     g.out = b.chunks;
     g.plane_c = b.plane_c;
     hg->push_back(g);
   }
-  // The grouped kernel deals tiles to CTAs round-robin in table order.
-  // Heaviest tiles first (digit pairs x k-steps x width: a quad-double tile
-  // carries ~4x the work of a double-double one, an octo-double tile ~15x),
-  // so that the deal approximates longest-processing-time-first and the
-  // CTAs finish together.  Only the order of the tiles changes; each still
-  // writes its own problem's chunk planes.
-  auto work = [](const mdgi::GroupedProblem &g) {
+  // work of one tile in k-steps of 128 x 128 output: digit pairs x k-blocks
+  // x tile area
+  auto tile_work = [&](const mdgi::GroupedProblem &g) {
     long long pairs = 0;
     for (int d = 0; d < g.D; ++d) pairs += mdgi::diag_pairs(d, g.s);
-    return pairs * g.KB * g.tn;
+    return pairs * g.KB * (pair ? 4 : g.tn / 128);
+  };
+  if (split) {
+    long long total = 0;
+    for (const mdgi::GroupedProblem &g : *hg) total += tile_work(g) * g.mt * g.nt;
+    const long long target =
+        std::max(1LL, total / ((long long)std::max(workers, 1) * kSplitUnitsPerWorker));
+    for (mdgi::GroupedProblem &g : *hg)
+      g.parts = (int)std::min<long long>(g.D, std::max(1LL, (tile_work(g) + target - 1) / target));
+  }
+  // The grouped kernel deals units to CTAs round-robin in table order.
+  // Heaviest units first (a quad-double tile carries ~4x the work of a
+  // double-double one, an octo-double tile ~15x), so that the deal
+  // approximates longest-processing-time-first and the CTAs finish
+  // together; a problem's units stay consecutive.  Only the order changes;
+  // each unit still writes its own problem's chunk planes.
+  auto unit_work = [&](const mdgi::GroupedProblem &g) {
+    return (tile_work(g) + g.parts - 1) / g.parts;
   };
   std::stable_sort(hg->begin(), hg->end(),
                    [&](const mdgi::GroupedProblem &a, const mdgi::GroupedProblem &b) {
-                     return work(a) > work(b);
+                     return unit_work(a) > unit_work(b);
                    });
-  int t = 0;
+  long long u = 0;
   for (mdgi::GroupedProblem &g : *hg) {
-    g.tile_begin = t;
-    t += g.mt * g.nt;
+    g.unit_begin = (int)u;
+    u += (long long)g.mt * g.nt * g.parts;
   }
-  *total_tiles = t;
+  if (u > (1LL << 30)) return MDG_ERROR_INVALID_SIZE;
+  *total_units = (int)u;
   return MDG_SUCCESS;
 }
 
@@ -225,17 +248,22 @@ std::string batch_key(const std::vector<BatchProblem> &hp) {
   return buf;
 }
 
-// Builds and uploads the grouped GEMM's table for a tile policy; waits for
-// the copy (the host table is a local).
-int apply_tiles(mdg_batch_s *h, int policy, cudaStream_t st) {
+// Builds and uploads the grouped GEMM's table for a tile policy and split
+// mode; waits for the copy (the host table is a local).
+int apply_tiles(mdg_batch_s *h, int policy, int split, cudaStream_t st) {
+  int dev = 0, sms = 0;
+  MDG_TRY_CUDA(cudaGetDevice(&dev));
+  MDG_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   std::vector<mdgi::GroupedProblem> hg;
-  int tiles = 0;
-  MDG_TRY(grouped_table(h->hprobs, policy, &hg, &tiles));
+  int units = 0;
+  MDG_TRY(grouped_table(h->hprobs, policy, split,
+                        policy == MDG_BATCH_TILES_PAIR ? sms / 2 : sms, &hg, &units));
   MDG_TRY_CUDA(cudaMemcpyAsync(h->dgroups, hg.data(), sizeof(mdgi::GroupedProblem) * h->count,
                                cudaMemcpyHostToDevice, st));
   MDG_TRY_CUDA(cudaStreamSynchronize(st));
-  h->total_tiles = tiles;
+  h->total_units = units;
   h->tiles_policy = policy;
+  h->split = split;
   return MDG_SUCCESS;
 }
 
@@ -272,12 +300,10 @@ int mdg_batch_create(const mdg_problem *problems, int count, void *workspace,
   h->dgroups = reinterpret_cast<mdgi::GroupedProblem *>(ws + L.off_groups);
   h->exps = reinterpret_cast<int *>(ws + L.off_exps);
   cudaStream_t s = mdgi::as_stream(stream);
-  // a tile policy tuned earlier for the same shapes, else 256-column tiles
-  // (on the 256-problem workload they ran 2 % faster than auto and 5 %
-  // faster than 128-column tiles: the single-CTA engine is bound by the
-  // operand bytes it streams per product, which narrower tiles raise)
-  int policy = MDG_BATCH_TILES_256;
-  mdgi::tune_lookup_batch(batch_key(h->hprobs), &policy);
+  // a tile policy and split mode tuned earlier for the same shapes, else
+  // 256-column tiles, split
+  int policy = MDG_BATCH_TILES_256, split = 1;
+  mdgi::tune_lookup_batch(batch_key(h->hprobs), &policy, &split);
   cudaError_t e = cudaMemcpyAsync(h->dprobs, h->hprobs.data(), sizeof(BatchProblem) * count,
                                   cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) {
@@ -285,7 +311,7 @@ int mdg_batch_create(const mdg_problem *problems, int count, void *workspace,
     delete h;
     return MDG_ERROR_CUDA;
   }
-  st = apply_tiles(h, policy, s);
+  st = apply_tiles(h, policy, split, s);
   if (st != MDG_SUCCESS) {
     delete h;
     return st;
@@ -307,7 +333,7 @@ int mdg_batch_run(mdg_batch_s *h, void *stream) {
     default: MDG_BATCH_STAGES(16); break;
   }
 #undef MDG_BATCH_STAGES
-  MDG_TRY(mdgi::launch_diag_gemm_grouped(h->dgroups, h->count, h->total_tiles,
+  MDG_TRY(mdgi::launch_diag_gemm_grouped(h->dgroups, h->count, h->total_units,
                                          h->tiles_policy == MDG_BATCH_TILES_PAIR, st));
   const int *rb = h->renorm_begin, *rc = h->renorm_count, *rn = h->renorm_n;
   MDG_TRY(mdgi::launch_batch_renorm<2>(h->dprobs, h->count, rb[0], rc[0], rn[0], h->exps, st));
@@ -320,10 +346,18 @@ int mdg_batch_run(mdg_batch_s *h, void *stream) {
 int mdg_batch_set_tiles(mdg_batch_s *h, int policy, void *stream) {
   if (!h) return MDG_ERROR_NULL_POINTER;
   if (policy < MDG_BATCH_TILES_AUTO || policy > MDG_BATCH_TILES_PAIR) return MDG_ERROR_INVALID_FORM;
-  return apply_tiles(h, policy, mdgi::as_stream(stream));
+  return apply_tiles(h, policy, h->split, mdgi::as_stream(stream));
 }
 
 int mdg_batch_tiles(mdg_batch_s *h) { return h ? h->tiles_policy : -1; }
+
+int mdg_batch_set_split(mdg_batch_s *h, int split, void *stream) {
+  if (!h) return MDG_ERROR_NULL_POINTER;
+  if (split != 0 && split != 1) return MDG_ERROR_INVALID_FORM;
+  return apply_tiles(h, h->tiles_policy, split, mdgi::as_stream(stream));
+}
+
+int mdg_batch_split(mdg_batch_s *h) { return h ? h->split : -1; }
 
 int mdg_batch_tune(mdg_batch_s *h, void *stream) {
   if (!h) return MDG_ERROR_NULL_POINTER;
@@ -332,11 +366,13 @@ int mdg_batch_tune(mdg_batch_s *h, void *stream) {
   cudaEvent_t e0, e1;
   MDG_TRY_CUDA(cudaEventCreate(&e0));
   MDG_TRY_CUDA(cudaEventCreate(&e1));
-  int best = h->tiles_policy, status = MDG_SUCCESS;
+  int best = h->tiles_policy, best_split = h->split, status = MDG_SUCCESS;
   float best_ms = 0.0f;
-  for (int policy : {MDG_BATCH_TILES_256, MDG_BATCH_TILES_AUTO, MDG_BATCH_TILES_128,
-                     MDG_BATCH_TILES_PAIR}) {
-    status = apply_tiles(h, policy, st);
+  for (int choice = 0; choice < 8 && status == MDG_SUCCESS; ++choice) {
+    static const int kPolicies[4] = {MDG_BATCH_TILES_256, MDG_BATCH_TILES_AUTO,
+                                     MDG_BATCH_TILES_128, MDG_BATCH_TILES_PAIR};
+    const int policy = kPolicies[choice >> 1], split = 1 - (choice & 1);
+    status = apply_tiles(h, policy, split, st);
     if (status == MDG_SUCCESS) status = mdg_batch_run(h, stream);  // warm-up
     if (status != MDG_SUCCESS) break;
     cudaEventRecord(e0, st);
@@ -352,14 +388,15 @@ int mdg_batch_tune(mdg_batch_s *h, void *stream) {
     if (best_ms == 0.0f || ms < best_ms) {
       best_ms = ms;
       best = policy;
+      best_split = split;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   MDG_TRY(status);
   MDG_TRY(mdg_device_status());  // a bounded wait that gave up fails the tuning
-  MDG_TRY(apply_tiles(h, best, st));
-  mdgi::tune_record_batch(batch_key(h->hprobs), best, best_ms);
+  MDG_TRY(apply_tiles(h, best, best_split, st));
+  mdgi::tune_record_batch(batch_key(h->hprobs), best, best_split, best_ms);
   return MDG_SUCCESS;
 }
 

@@ -208,13 +208,36 @@ __device__ __forceinline__ void drain128(uint32_t taddr, int (&acc)[128]) {
   add_exact(acc + 96, rb);
 }
 
-// One tile of work: where its operands and output live and which of its
-// problem's rows / columns it covers.  tn: tile width, 256 or 128 columns
-// (the B box of tmB is tn rows); ktail: MMAs of K = 16 issued for the last
-// k-block (1..4; the rest of that block is the zero padding of k).
+// Diagonals [d0, d1) of part `part` of a tile cut into `parts` ranges whose
+// digit-pair counts add up to about 1/parts of the tile's pairs each (empty
+// when parts exceeds what the pair counts allow).
+__device__ __forceinline__ void part_diagonals(int s, int D, int part, int parts, int &d0,
+                                               int &d1) {
+  int total = 0;
+  for (int d = 0; d < D; ++d) total += mdgi::diag_pairs(d, s);
+  const long long lo = (long long)total * part / parts, hi = (long long)total * (part + 1) / parts;
+  int cum = 0;
+  d0 = D;
+  d1 = D;
+  for (int d = 0; d < D; ++d) {
+    if (cum >= lo && d0 == D) d0 = d;
+    if (cum >= hi) {
+      d1 = d;
+      break;
+    }
+    cum += mdgi::diag_pairs(d, s);
+  }
+  if (d0 > d1) d0 = d1;
+}
+
+// One unit of work: where its operands and output live, which of its
+// problem's rows / columns it covers and which diagonals [d0, d1) it
+// computes.  tn: tile width, 256 or 128 columns (the B box of tmB is tn
+// rows); ktail: MMAs of K = 16 issued for the last k-block (1..4; the rest
+// of that block is the zero padding of k).
 struct TileJob {
   const CUtensorMap *tmA, *tmB;
-  int s, D, Mp, Np, KB, row, col, tn, ktail;
+  int s, D, Mp, Np, KB, row, col, tn, ktail, d0, d1;
   int *out;
   long long plane_c;
 };
@@ -229,7 +252,7 @@ struct SingleJobs {
   __device__ TileJob job(int t) const {
     const int MB = Mp / TM;
     return TileJob{tmA, tmB, s, D, Mp, Np, KB, (t % MB) * TM, (t / MB) * TN, TN, TK / 16,
-                   out, plane_c};
+                   0, D, out, plane_c};
   }
 };
 
@@ -289,7 +312,7 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
       for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const TileJob jb = jobs.job(tile);
         const int s = jb.s, KB = jb.KB;
-        for (int d = 0; d < jb.D; ++d) {
+        for (int d = jb.d0; d < jb.d1; ++d) {
           const int ilo = d - (s - 1) > 0 ? d - (s - 1) : 0;
           const int S = mdgi::diag_pairs(d, s) * KB;
           for (int t = 0; t < S; ++t) {
@@ -322,7 +345,7 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
       for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const TileJob jb = jobs.job(tile);
         const uint32_t idesc = (IDESC & ~(0x3Fu << 17)) | ((uint32_t)(jb.tn >> 3) << 17);
-        for (int d = 0; d < jb.D; ++d) {
+        for (int d = jb.d0; d < jb.d1; ++d) {
           const int S = mdgi::diag_pairs(d, jb.s) * jb.KB;
           int kb = 0;  // k-block of step t within its digit pair
           for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
@@ -382,7 +405,8 @@ __device__ __forceinline__ void tc1_body(const Jobs &jobs) {
       const int row = jb.row + 32 * q + lane;
       const int col = jb.col + 128 * h;
       int chunk = 0;
-      for (int d = 0; d < jb.D; ++d) {
+      for (int d = 0; d < jb.d0; ++d) chunk += mdgi::diag_chunks(d, jb.s, jb.KB);
+      for (int d = jb.d0; d < jb.d1; ++d) {
         const int S = mdgi::diag_pairs(d, jb.s) * jb.KB;
         for (int g0 = 0; g0 < S; g0 += mdgi::GROUP_STEPS) {
           // lane 0 waits; the outcome is broadcast so the warp stays
@@ -437,22 +461,33 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 // Many problems: a table of GroupedProblem in global memory (tensor maps
-// included, 64-byte aligned), tiles numbered problem after problem.
+// included, 64-byte aligned), units numbered problem after problem and,
+// within a problem, part after part (all tiles of one diagonal range, then
+// the next range).
+__device__ __forceinline__ const mdgi::GroupedProblem &grouped_find(
+    const mdgi::GroupedProblem *probs, int count, int u) {
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (probs[mid].unit_begin <= u) lo = mid; else hi = mid - 1;
+  }
+  return probs[lo];
+}
+
 struct GroupedJobs {
   const mdgi::GroupedProblem *probs;
   int count, total;
   __device__ int tiles() const { return total; }
-  __device__ TileJob job(int t) const {
-    int lo = 0, hi = count - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (probs[mid].tile_begin <= t) lo = mid; else hi = mid - 1;
-    }
-    const mdgi::GroupedProblem &g = probs[lo];
-    const int lt = t - g.tile_begin;
+  __device__ TileJob job(int u) const {
+    const mdgi::GroupedProblem &g = grouped_find(probs, count, u);
+    const int lt = u - g.unit_begin, tiles = g.mt * g.nt;
+    const int tile = lt % tiles, part = lt / tiles;
+    int d0, d1;
+    part_diagonals(g.s, g.D, part, g.parts, d0, d1);
     return TileJob{reinterpret_cast<const CUtensorMap *>(g.tmA),
                    reinterpret_cast<const CUtensorMap *>(g.tmB), g.s, g.D, g.Mp, g.Np, g.KB,
-                   (lt % g.mt) * TM, (lt / g.mt) * g.tn, g.tn, g.ktail, g.out, g.plane_c};
+                   (tile % g.mt) * TM, (tile / g.mt) * g.tn, g.tn, g.ktail, d0, d1, g.out,
+                   g.plane_c};
   }
 };
 
@@ -603,19 +638,8 @@ struct PairSingle {
   __device__ PairJob job(int u) const {
     const int MB = Mp / 256, NB = Np / TN2, tiles = MB * NB;
     const int tile = u % tiles, part = u / tiles;
-    int total = 0;
-    for (int d = 0; d < D; ++d) total += mdgi::diag_pairs(d, s);
-    const long long lo = (long long)total * part / parts, hi = (long long)total * (part + 1) / parts;
-    int cum = 0, d0 = D, d1 = D;
-    for (int d = 0; d < D; ++d) {
-      if (cum >= lo && d0 == D) d0 = d;
-      if (cum >= hi) {
-        d1 = d;
-        break;
-      }
-      cum += mdgi::diag_pairs(d, s);
-    }
-    if (d0 > d1) d0 = d1;
+    int d0, d1;
+    part_diagonals(s, D, part, parts, d0, d1);
     const int strip = tile / (MB * raster);
     const int idx = tile - strip * MB * raster;
     const int c0 = strip * raster;
@@ -626,23 +650,21 @@ struct PairSingle {
 };
 
 // Many problems (GroupedProblem table in global memory, tensor maps with
-// 128-row boxes for A and B, Mp a multiple of 256): units are whole 256 x 256
-// tiles, numbered problem after problem (mt row tiles x nt column tiles each).
+// 128-row boxes for A and B, Mp a multiple of 256): units are 256 x 256
+// tiles times diagonal ranges, numbered as for the single-CTA kernel.
 struct PairGrouped {
   const mdgi::GroupedProblem *probs;
   int count, total;
   __device__ int units() const { return total; }
   __device__ PairJob job(int u) const {
-    int lo = 0, hi = count - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (probs[mid].tile_begin <= u) lo = mid; else hi = mid - 1;
-    }
-    const mdgi::GroupedProblem &g = probs[lo];
-    const int lt = u - g.tile_begin;
+    const mdgi::GroupedProblem &g = grouped_find(probs, count, u);
+    const int lt = u - g.unit_begin, tiles = g.mt * g.nt;
+    const int tile = lt % tiles, part = lt / tiles;
+    int d0, d1;
+    part_diagonals(g.s, g.D, part, g.parts, d0, d1);
     return PairJob{reinterpret_cast<const CUtensorMap *>(g.tmA),
                    reinterpret_cast<const CUtensorMap *>(g.tmB), g.s, g.D, g.Mp, g.Np, g.KB,
-                   (lt % g.mt) * 256, (lt / g.mt) * TN2, 0, g.D, g.out, g.plane_c};
+                   (tile % g.mt) * 256, (tile / g.mt) * TN2, d0, d1, g.out, g.plane_c};
   }
 };
 
@@ -1031,9 +1053,9 @@ int encode_plane_map(void *map128, const void *base, int Kp, long long rows_tota
   return make_map(reinterpret_cast<CUtensorMap *>(map128), base, Kp, rows_total, box_rows);
 }
 
-int launch_diag_gemm_grouped(const GroupedProblem *dev_probs, int count, int total_tiles,
+int launch_diag_gemm_grouped(const GroupedProblem *dev_probs, int count, int total_units,
                              int pair, cudaStream_t st) {
-  if (total_tiles == 0) return MDG_SUCCESS;
+  if (total_units == 0) return MDG_SUCCESS;
   int dev = 0, sms = 0;
   MDG_TRY_CUDA(cudaGetDevice(&dev));
   MDG_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1041,15 +1063,15 @@ int launch_diag_gemm_grouped(const GroupedProblem *dev_probs, int count, int tot
     MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc2_grouped_kernel,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
     const int ncl = sms / 2;
-    const int clusters = total_tiles < ncl ? total_tiles : ncl;
+    const int clusters = total_units < ncl ? total_units : ncl;
     diag_gemm_tc2_grouped_kernel<<<2 * clusters, THREADS2, SMEM2_BYTES, st>>>(dev_probs, count,
-                                                                            total_tiles);
+                                                                            total_units);
   } else {
     MDG_TRY_CUDA(cudaFuncSetAttribute(diag_gemm_tc_grouped_kernel,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    const int grid = total_tiles < sms ? total_tiles : sms;
+    const int grid = total_units < sms ? total_units : sms;
     diag_gemm_tc_grouped_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(dev_probs, count,
-                                                                   total_tiles);
+                                                                   total_units);
   }
   MDG_TRY_LAUNCH();
   return MDG_SUCCESS;

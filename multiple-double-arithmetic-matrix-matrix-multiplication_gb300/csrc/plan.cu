@@ -12,8 +12,8 @@
 // <Kp>", the padded sizes the kernels see); mdg_tune_cache_save / _load keep
 // it as a small JSON file.  Slice and diagonal counts change the rounding, so
 // they stay the caller's options and are part of the key, not tuned.  The
-// batched plan (batched.cu) records its tile policy here too, under "batch
-// <count> <hash of the problem shapes>".
+// batched plan (batched.cu) records its tile policy and split mode here
+// too, under "batch <count> <hash of the problem shapes>".
 #include <cctype>
 #include <cstdio>
 #include <cstdlib>
@@ -27,9 +27,9 @@
 namespace {
 
 // A single-problem schedule (engine, parts, raster, pace), or for a batched
-// plan ("batch ..." keys) its tile policy.
+// plan ("batch ..." keys) its tile policy and split mode (-1: not recorded).
 struct TuneEntry {
-  int engine = 0, parts = 0, raster = 0, pace = 0, tiles = 0;
+  int engine = 0, parts = 0, raster = 0, pace = 0, tiles = 0, split = -1;
   double ms = 0.0;
 };
 
@@ -128,22 +128,25 @@ std::string quoted(const std::string &s) {
 
 namespace mdgi {
 
-void tune_lookup_batch(const std::string &key, int *policy) {
+void tune_lookup_batch(const std::string &key, int *policy, int *split) {
   std::string dev;
   if (device_key(&dev) != MDG_SUCCESS) return;
   std::lock_guard<std::mutex> lk(g_tune_mu);
   auto d = g_tune.find(dev);
   if (d == g_tune.end()) return;
   auto e = d->second.find(key);
-  if (e != d->second.end()) *policy = e->second.tiles;
+  if (e == d->second.end()) return;
+  *policy = e->second.tiles;
+  if (e->second.split >= 0) *split = e->second.split;
 }
 
-void tune_record_batch(const std::string &key, int policy, double ms) {
+void tune_record_batch(const std::string &key, int policy, int split, double ms) {
   std::string dev;
   if (device_key(&dev) != MDG_SUCCESS) return;
   std::lock_guard<std::mutex> lk(g_tune_mu);
   TuneEntry &t = g_tune[dev][key];
   t.tiles = policy;
+  t.split = split;
   t.ms = ms;
 }
 
@@ -316,6 +319,7 @@ int mdg_tune_cache_load(const char *path) {
         if (field == "raster") return whole_in(v, 0, 1 << 20, &e.raster);
         if (field == "pace") return whole_in(v, -1, 65536, &e.pace);
         if (field == "tiles") return whole_in(v, 0, 3, &e.tiles);
+        if (field == "split") return whole_in(v, 0, 1, &e.split);
         if (field == "ms") {
           if (!(v >= 0.0 && v <= 1e12)) return false;
           e.ms = v;
@@ -346,7 +350,10 @@ int mdg_tune_cache_save(const char *path) {
       bool first = true;
       for (auto &e : d.second) {
         char buf[160];
-        if (e.first.compare(0, 6, "batch ") == 0)
+        if (e.first.compare(0, 6, "batch ") == 0 && e.second.split >= 0)
+          std::snprintf(buf, sizeof(buf), "{\"tiles\": %d, \"split\": %d, \"ms\": %.4f}",
+                        e.second.tiles, e.second.split, e.second.ms);
+        else if (e.first.compare(0, 6, "batch ") == 0)
           std::snprintf(buf, sizeof(buf), "{\"tiles\": %d, \"ms\": %.4f}", e.second.tiles,
                         e.second.ms);
         else

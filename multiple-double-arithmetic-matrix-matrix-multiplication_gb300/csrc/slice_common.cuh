@@ -54,41 +54,40 @@ __device__ __forceinline__ uint64_t wide_bits64(const uint64_t (&w)[NW], int pos
   return r ? ((lo >> r) | (hi << (64 - r))) : lo;
 }
 
-// Index of the highest set bit of a non-negative w, -1 for zero.
+// Bits [pos, pos + 128) of w (0 <= pos < 64 NW) as lo and hi; bits above the
+// top word read as the sign.  The same barrel shift as wide_bits64, over
+// one more word.
 template <int NW>
-__device__ __forceinline__ int wide_msb(const uint64_t (&w)[NW]) {
-  int t = -1;
-#pragma unroll
-  for (int i = 0; i < NW; ++i)
-    if (w[i]) t = i * 64 + 63 - __clzll((long long)w[i]);
-  return t;
-}
-
-// Any bit set strictly below position pos (pos >= 0)?  Masks instead of
-// selects on the word index, for the same reason as wide_bits64.
-template <int NW>
-__device__ __forceinline__ bool wide_any_below(const uint64_t (&w)[NW], int pos) {
+__device__ __forceinline__ void wide_bits128(const uint64_t (&w)[NW], int pos, uint64_t &lo,
+                                             uint64_t &hi) {
   const int qw = pos >> 6, r = pos & 63;
-  const uint64_t low = r ? ((1ull << r) - 1) : 0ull;
-  uint64_t acc = 0;
+  const uint64_t fill = (uint64_t)((int64_t)w[NW - 1] >> 63);
+  uint64_t t[NW + 2];
 #pragma unroll
-  for (int i = 0; i < NW; ++i) {
-    const uint64_t m_lt = 0ull - (uint64_t)(i < qw);
-    const uint64_t m_eq = 0ull - (uint64_t)(i == qw);
-    acc |= (w[i] & m_lt) | (w[i] & m_eq & low);
+  for (int i = 0; i < NW; ++i) t[i] = w[i];
+  t[NW] = fill;
+  t[NW + 1] = fill;
+#pragma unroll
+  for (int bit = 1; bit <= NW; bit <<= 1) {
+    const bool on = (qw & bit) != 0;
+#pragma unroll
+    for (int i = 0; i <= NW + 1; ++i) {
+      const uint64_t src = (i + bit <= NW + 1) ? t[i + bit] : fill;
+      t[i] = on ? src : t[i];
+    }
   }
-  return acc != 0;
+  lo = r ? ((t[0] >> r) | (t[1] << (64 - r))) : t[0];
+  hi = r ? ((t[1] >> r) | (t[2] << (64 - r))) : t[1];
 }
 
+// Index of the lowest set bit of w, 64 NW for zero.
 template <int NW>
-__device__ __forceinline__ void wide_neg(uint64_t (&w)[NW]) {
-  uint64_t carry = 1;
+__device__ __forceinline__ int wide_lsb(const uint64_t (&w)[NW]) {
+  int b = 64 * NW;
 #pragma unroll
-  for (int i = 0; i < NW; ++i) {
-    const uint64_t s = ~w[i] + carry;
-    carry = (carry && s == 0) ? 1 : 0;
-    w[i] = s;
-  }
+  for (int i = NW - 1; i >= 0; --i)
+    if (w[i]) b = 64 * i + __ffsll((long long)w[i]) - 1;
+  return b;
 }
 
 // x = m 2^e2 with m an integer, |m| < 2^53 (0 for x = +-0), read from the

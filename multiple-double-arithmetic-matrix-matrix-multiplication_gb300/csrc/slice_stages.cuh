@@ -179,6 +179,7 @@ __device__ __forceinline__ void digits_elem4(int P, int s, int rows, int cols,
 // bytes land at positions fixed at compile time, so W stays in registers.
 // Each thread takes V adjacent columns and loads their chunk sums as one
 // vector per chunk plane.
+// V adjacent int32 as one vector load.
 template <int V>
 struct IntV;
 template <>
@@ -200,34 +201,77 @@ struct IntV<1> {
   static __device__ __forceinline__ void load(const int *p, int (&x)[1]) { x[0] = *p; }
 };
 
-// The P limbs of W * 2^scale (W a wide integer, consumed): limb l is W,
-// rounded to nearest-even to 53 bits, then removed from W.
+// The P limbs of W * 2^scale (W a wide two's complement integer): limb l
+// is the residual R_l = W - (limbs 0..l-1), rounded to nearest-even to 53
+// bits.  W itself is never modified: after a limb rounded at bit sh, the
+// residual is W's bits below sh with every bit from sh up equal to f, where
+// f is all ones if that limb was rounded up and zero otherwise (rounding up
+// leaves a negative remainder, rounding down a non-negative one, and |R|
+// is below 2^sh either way).  So each limb needs: the highest bit of R
+// that differs from f (its magnitude), a 64-bit window of R at that bit,
+// and whether any bit of W lies below the rounding position (the sticky
+// bit, from W's lowest set bit, found once).  The search looks at a
+// 128-bit window of R ending at the current cut h and moves down 64 bits
+// at a time while the window's upper half carries nothing but f.
 template <int P, int NW>
-__device__ __forceinline__ void emit_limbs(uint64_t (&w)[NW], int scale, double *out) {
+__device__ __forceinline__ void emit_limbs(const uint64_t (&w)[NW], int scale, double *out) {
+  const int lsb = mdgi::wide_lsb<NW>(w);
+  uint64_t f = (uint64_t)((int64_t)w[NW - 1] >> 63);
+  int h = 64 * NW;  // bits of R from h up all equal f
 #pragma unroll 1
   for (int l = 0; l < P; ++l) {
-    const bool neg = (int64_t)w[NW - 1] < 0;
-    uint64_t mag[NW];
-#pragma unroll
-    for (int i = 0; i < NW; ++i) mag[i] = w[i];
-    if (neg) mdgi::wide_neg<NW>(mag);
-    const int tb = mdgi::wide_msb<NW>(mag);
-    if (tb < 0) {
+    if (f == 0 && lsb >= h) {  // R = 0
       out[l] = 0.0;
       continue;
     }
-    const int sh = tb > 52 ? tb - 52 : 0;
-    // one 64-bit window from bit sh - 1: the round bit, then the 53 bits
-    // of the limb (tb <= 52: the limb is word 0 itself, nothing to round)
-    const uint64_t x = sh > 0 ? mdgi::wide_bits64<NW>(mag, sh - 1) : (mag[0] << 1);
-    uint64_t mm = (x >> 1) & ((1ull << 53) - 1);
-    if (sh > 0 && (x & 1ull)) {
-      const bool sticky = sh > 1 && mdgi::wide_any_below<NW>(mag, sh - 1);
-      if (sticky || (mm & 1)) mm += 1;
+    int b0, t;
+    uint64_t lo, hi;
+    for (;;) {  // at most NW passes: h drops by 64 per pass
+      b0 = h > 128 ? h - 128 : 0;
+      mdgi::wide_bits128<NW>(w, b0, lo, hi);
+      const int cut = h - b0;  // 0..128: window bits from cut up are f
+      if (cut < 64) {
+        const uint64_t keep = cut ? ((1ull << cut) - 1) : 0ull;
+        lo = (lo & keep) | (f & ~keep);
+        hi = f;
+      } else if (cut < 128) {
+        const uint64_t keep = cut > 64 ? ((1ull << (cut - 64)) - 1) : 0ull;
+        hi = (hi & keep) | (f & ~keep);
+      }
+      const uint64_t xh = hi ^ f, xl = lo ^ f;
+      if (xh) {
+        t = b0 + 127 - __clzll((long long)xh);
+        break;
+      }
+      if (b0 == 0) {
+        t = xl ? 63 - __clzll((long long)xl) : -1;  // -1: R = -1
+        break;
+      }
+      h = b0 + 64;
     }
-    // mm 2^(sh + scale) as a double; with the top bit at 52 (or 53 after
-    // rounding up) and a normal exponent it is assembled from its fields
-    // by integer instructions, otherwise converted and scaled in FP64
+    // rounding position sh; x = bits [sh - 1, sh + 63) of R: the round bit,
+    // then m = floor(R / 2^sh), |m| <= 2^53 (sh = 0: R itself, b0 = 0)
+    const int sh = t > 52 ? t - 52 : 0;
+    uint64_t x;
+    if (sh == 0) {
+      x = lo << 1;
+    } else {
+      const int o = sh - 1 - b0;  // 0..127
+      if (o < 64)
+        x = o ? ((lo >> o) | (hi << (64 - o))) : lo;
+      else
+        x = o > 64 ? ((hi >> (o - 64)) | (f << (128 - o))) : hi;
+    }
+    const int64_t m = (int64_t)x >> 1;
+    const bool up = sh > 0 && (x & 1ull) && (lsb < sh - 1 || (m & 1));
+    const int64_t mr = up ? m + 1 : m;
+    f = up ? ~0ull : 0ull;
+    h = sh;
+    // mr 2^(sh + scale) as a double; with the top bit at 52 (or 53) and a
+    // normal exponent it is assembled from its fields by integer
+    // instructions, otherwise converted and scaled in FP64
+    const bool neg = mr < 0;
+    const uint64_t mm = neg ? (uint64_t)(-mr) : (uint64_t)mr;
     const bool top = mm >> 53;
     const uint64_t frac = top ? (mm >> 1) : mm;
     const int be = sh + scale + 52 + (top ? 1 : 0) + 1023;
@@ -237,7 +281,6 @@ __device__ __forceinline__ void emit_limbs(uint64_t (&w)[NW], int scale, double 
     else
       val = ldexp((double)mm, sh + scale);
     out[l] = neg ? -val : val;
-    mdgi::wide_add_shifted<NW>(w, neg ? (int64_t)mm : -(int64_t)mm, sh);
   }
 }
 

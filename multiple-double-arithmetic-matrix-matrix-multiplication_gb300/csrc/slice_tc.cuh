@@ -89,25 +89,29 @@ int launch_renorm(int p, int s, int D, int KB, int m, int n, const int *chunks,
 // One problem of a grouped diagonal GEMM: the single-CTA tcgen05 kernel
 // (tiles of 128 rows x tn columns, tn = 256 or 128) or the CTA-pair kernel
 // (tiles of 256 x 256; B box of 128 rows, one half per CTA).  Tensor maps of
-// its digit planes, sizes, first global tile, row tiles mt and column tiles
-// nt, output chunk planes.  ktail: MMAs of K = 16 that reach data in the last
-// 64-deep k-block (1..4; single-CTA kernel).  Lives in global memory,
-// 64-byte aligned.
+// its digit planes, sizes, first global work unit, row tiles mt and column
+// tiles nt, parts per tile, output chunk planes.  The problem's units are
+// its mt x nt tiles times `parts` ranges of diagonals (whose digit-pair
+// counts add up to about 1/parts of a tile's pairs each), numbered part
+// after part.  ktail: MMAs of K = 16 that reach data in the last 64-deep
+// k-block (1..4; single-CTA kernel).  Lives in global memory, 64-byte
+// aligned.
 struct alignas(64) GroupedProblem {
   unsigned char tmA[128];  // CUtensorMap, A planes, box 64 x 128
   unsigned char tmB[128];  // CUtensorMap, B planes, box 64 x tn (pairs: 64 x 128)
-  int s, D, Mp, Np, KB, tile_begin, tn, mt, nt, ktail;
+  int s, D, Mp, Np, KB, unit_begin, tn, mt, nt, ktail, parts;
   int *out;
   long long plane_c;
 };
 int encode_plane_map(void *map128, const void *base, int Kp, long long rows_total, int box_rows);
 // The batched plan's entries in the tuning cache (plan.cu), under the
-// current device: the tile policy recorded for a batch key, if any
-// (*policy is left alone otherwise), and a new record.
-void tune_lookup_batch(const std::string &key, int *policy);
-void tune_record_batch(const std::string &key, int policy, double ms);
+// current device: the tile policy and split mode recorded for a batch key,
+// if any (left alone otherwise; a record without a split mode sets only the
+// policy), and a new record.
+void tune_lookup_batch(const std::string &key, int *policy, int *split);
+void tune_record_batch(const std::string &key, int policy, int split, double ms);
 // pair: the CTA-pair kernel (Mp of every problem a multiple of 256).
-int launch_diag_gemm_grouped(const GroupedProblem *dev_probs, int count, int total_tiles,
+int launch_diag_gemm_grouped(const GroupedProblem *dev_probs, int count, int total_units,
                              int pair, cudaStream_t st);
 
 // Waits for the device; MDG_ERROR_TIMEOUT if a bounded wait of the tcgen05

@@ -195,6 +195,8 @@ def test_batch_plan_sizes_and_arguments(L):
     assert L.mdg_batch_create(t, 4, ctypes.c_void_p(256), full - 1, None, ctypes.byref(h)) == 5
     assert not h.value
     assert L.mdg_batch_run(None, None) == 3
+    assert L.mdg_batch_set_split(None, 1, None) == 3 and L.mdg_batch_split(None) == -1
+    assert L.mdg_batch_set_tiles(None, 1, None) == 3 and L.mdg_batch_tiles(None) == -1
     L.mdg_batch_destroy(None)
     assert L.mdg_gemm_batched(2, t, -1, None, None, 0, None) == 2
     assert L.mdg_gemm_batched(2, t, 0, None, None, 0, None) == 0

@@ -576,11 +576,13 @@ def test_batched_plan_graph_capture(api, orc, inputs):
 
 def test_batched_tile_policies_bit_identical_and_tuned(api, orc, inputs):
     """The grouped GEMM under each tile policy (256-column tiles, 128-column
-    tiles, the per-problem choice, and 256 x 256 tiles on CTA pairs) over
+    tiles, the per-problem choice, and 256 x 256 tiles on CTA pairs) and
+    split mode (heavy tiles cut into diagonal ranges, down to ranges that
+    hold no diagonal for the hexa-double problem, or whole tiles) over
     problems whose n falls on both
     sides of a 256 boundary and whose k ends inside a 64-deep block (the
     last block issues fewer MMAs): every problem's C equals the
-    single-problem GEMM under every policy; tuning keeps one of them and
+    single-problem GEMM under every choice; tuning keeps one of them and
     records it for plans of the same shapes."""
     rng = np.random.default_rng(31)
     probs = [(2, 96, 300, 40), (4, 130, 100, 96), (8, 64, 384, 160), (2, 256, 512, 16),
@@ -589,21 +591,23 @@ def test_batched_tile_policies_bit_identical_and_tuned(api, orc, inputs):
            for P, m, n, k in probs]
     want = [api.gemm(A, B, "slice_bf16") for A, B in ops]
     plan = api.BatchPlan(ops)
-    assert plan.tiles == "256"
-    for policy in ("auto", "128", "pair", "256"):
-        plan.set_tiles(policy)
-        for C in plan.Cs:
-            C.fill_(np.nan)
-        plan.run()
-        torch.cuda.synchronize()
-        for i, (C, W) in enumerate(zip(plan.Cs, want)):
-            assert torch.equal(C, W), (policy, probs[i])
+    assert plan.tiles == "256" and plan.split
+    for split in (True, False):
+        plan.set_split(split)
+        for policy in ("auto", "128", "pair", "256"):
+            plan.set_tiles(policy)
+            for C in plan.Cs:
+                C.fill_(np.nan)
+            plan.run()
+            torch.cuda.synchronize()
+            for i, (C, W) in enumerate(zip(plan.Cs, want)):
+                assert torch.equal(C, W), (policy, split, probs[i])
     api.tune_cache_clear()
     best = plan.tune()
     assert best in ("auto", "256", "128", "pair")
     assert api.tune_cache_size() == 1
-    again = api.BatchPlan(ops)  # same shapes: starts with the tuned policy
-    assert again.tiles == best
+    again = api.BatchPlan(ops)  # same shapes: starts with the tuned choice
+    assert again.tiles == best and again.split == plan.split
     again.run()
     torch.cuda.synchronize()
     for C, W in zip(again.Cs, want):

@@ -14,7 +14,9 @@ CACHE = {"NVIDIA GB300|13000": {"2 4 28 28 1024 1024 1024": {"engine": 2, "parts
                                                             "ms": 1.25},
                                 "2 2 14 14 256 256 64": {"engine": 1, "parts": 0,
                                                         "raster": 0, "pace": -1, "ms": 0.01},
-                                "batch 256 0123456789abcdef": {"tiles": 2, "ms": 13.5}},
+                                "batch 256 0123456789abcdef": {"tiles": 2, "ms": 13.5},
+                                "batch 7 fedcba9876543210": {"tiles": 3, "split": 0,
+                                                             "ms": 0.5}},
          "other|1": {}}
 
 
@@ -24,13 +26,13 @@ def test_tune_cache_json_round_trip(tmp_path):
     src = tmp_path / "in.json"
     src.write_text(json.dumps(CACHE))
     api.tune_cache_load(src)
-    assert api.tune_cache_size() == 3
+    assert api.tune_cache_size() == 4
     out = tmp_path / "out.json"
     api.tune_cache_save(out)
     back = json.loads(out.read_text())
     assert back["NVIDIA GB300|13000"] == CACHE["NVIDIA GB300|13000"]
     api.tune_cache_load(out)  # merging the same entries again changes nothing
-    assert api.tune_cache_size() == 3
+    assert api.tune_cache_size() == 4
     api.tune_cache_clear()
     assert api.tune_cache_size() == 0
 
@@ -46,6 +48,7 @@ def test_tune_cache_rejects_bad_files(tmp_path):
                          ("engine", "nan"), ("parts", "9"), ("parts", "1.5"),
                          ("raster", "-1"), ("raster", "inf"), ("raster", "2e6"),
                          ("tiles", "4"), ("tiles", "-1"), ("pace", "-2"), ("pace", "70000"),
+                         ("split", "2"), ("split", "-1"),
                          ("ms", "-1"), ("ms", "nan")):
         bad.write_text('{"d": {"ok": {"engine": 2, "parts": 1}, '
                        f'"s": {{"{field}": {value}}}}}}}')
