@@ -289,8 +289,11 @@ int mdg_slice_digits(int p, int s, int rows, int cols, const double *X,
 
 /* Number of int32 chunk planes mdg_slice_diagonals writes: the products
  * of diagonal d (its digit pairs times k/64 steps of 64) are cut into runs
- * of 1024 steps, so each chunk holds at most 65536 products of magnitude
- * <= 2^14 and its sum is an exact int32 with |sum| <= 2^30. */
+ * of 2032 steps, so each chunk holds at most 130048 products of magnitude
+ * <= 2^14 and its sum is an exact int32 with |sum| <= 2032 * 2^20 < 2^31.
+ * Diagonal d has mdg_slice_chunk_count(s, d + 1, k) -
+ * mdg_slice_chunk_count(s, d, k) of them (0 for d = 0), numbered diagonal
+ * by diagonal. */
 int mdg_slice_chunk_count(int s, int D, int k);
 
 /* Exact diagonal sums on BF16 tensor cores: for d < D the sum over i+j=d

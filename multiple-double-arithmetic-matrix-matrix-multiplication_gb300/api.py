@@ -428,13 +428,13 @@ def slice_diagonals(dA, dB, D):
 
 
 def chunks_to_diagonals(Cd, s, D, k):
-    """Sum the chunk planes of each diagonal (int64), host side."""
-    KB = -(-max(k, 1) // 64)
+    """Sum the chunk planes of each diagonal (int64), host side; the
+    library says how many planes each diagonal has."""
+    count = lib().mdg_slice_chunk_count
     out, q = [], 0
     x = Cd.cpu().numpy().astype(np.int64)
     for d in range(D):
-        lo, hi = max(0, d - (s - 1)), min(d, s - 1)
-        nc = -(-((hi - lo + 1) * KB) // 1024)
+        nc = count(s, d + 1, k) - (count(s, d, k) if d else 0)
         out.append(x[q:q + nc].sum(axis=0))
         q += nc
     return np.stack(out)

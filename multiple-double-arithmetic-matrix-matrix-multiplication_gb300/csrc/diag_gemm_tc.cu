@@ -4,7 +4,7 @@
 // the products A_i B_j^T with i + j = d are summed over k exactly: BF16
 // digits in [-128, 128], FP32 accumulation in tensor memory (TMEM), flushed
 // every 1024 products (|partial| <= 2^24) into int32 registers, stored every
-// 65536 products as one int32 chunk plane (|sum| <= 2^30).
+// 2032 k-steps (130048 products) as one int32 chunk plane (|sum| < 2^31).
 //
 // One CTA per SM, persistent over tiles; 10 warps with fixed roles:
 //   warp 0      TMA producer: A_i (128 x 64) and B_j (256 x 64) k-blocks

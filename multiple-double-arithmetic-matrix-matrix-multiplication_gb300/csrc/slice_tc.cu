@@ -13,9 +13,8 @@
 //    of two digits is at most 2^14, so an FP32 accumulator holds the exact
 //    sum of 1024 of them (|sum| <= 2^24); every 1024 products (256 in the
 //    mma.sync engine) the FP32 accumulator is flushed into 32-bit
-//    integers, and every 65536 products
-//    the integers are stored as one "chunk" plane (|sum| <= 2^30).  All
-//    sums are exact.
+//    integers, and every 2032 k-steps (130048 products) the integers are
+//    stored as one "chunk" plane (|sum| < 2^31).  All sums are exact.
 // 4. renormalisation.  W = sum_d C_d 256^(D-1-d), C_d the sum of the
 //    chunks of diagonal d, is formed exactly in
 //    wide integers and rounded to P limbs, each to nearest, scaled by

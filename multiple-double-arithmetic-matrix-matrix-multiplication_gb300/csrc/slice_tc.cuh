@@ -10,10 +10,12 @@ namespace mdgi {
 
 // The diagonal sums are written as int32 "chunk" planes: the products of
 // diagonal d (pairs_d digit pairs times Kp/64 k-steps of 64) are cut into
-// runs of CHUNK_STEPS k-steps, at most 65536 products of |d_i d_j| <= 2^14,
-// so every chunk sum is an exact int32 with |sum| <= 2^30.  Chunks are
-// numbered diagonal by diagonal.
-constexpr int CHUNK_STEPS = 1024;
+// runs of CHUNK_STEPS k-steps, at most 2032 x 64 = 130048 products of
+// |d_i d_j| <= 2^14, so every chunk sum is an exact int32 with |sum| <=
+// 2032 x 2^20 = 2130706432 < 2^31.  2032 is the longest run of 16-step
+// flush groups that int32 holds: fewer chunk planes to write and to read
+// back.  Chunks are numbered diagonal by diagonal.
+constexpr int CHUNK_STEPS = 2032;
 // k-steps of 64 per FP32 accumulator flush in the tcgen05 engines: 1024
 // products of magnitude <= 2^14, so every partial sum is an integer with
 // |sum| <= 2^24, exactly representable in FP32.

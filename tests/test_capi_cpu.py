@@ -87,6 +87,18 @@ def test_workspace_sizes(L):
     assert api.workspace_size("slice_bf16", 4, 64, 64, 64, slices=200) == 0
 
 
+def test_chunk_counts(L):
+    """Diagonal d (pairs_d digit pairs, k/64 steps each) is cut into int32
+    chunks of at most 2032 steps: quad-double at k = 8192 has 15 diagonals
+    of one chunk and 13 of two."""
+    count = L.mdg_slice_chunk_count
+    assert count(1, 1, 2032 * 64) == 1 and count(1, 1, 2032 * 64 + 1) == 2
+    assert count(1, 1, 2 * 2032 * 64 + 640) == 3
+    assert count(28, 28, 8192) == 15 + 2 * 13
+    assert count(28, 28, 0) == 28  # k = 0: one (empty) step per pair
+    assert count(28, 56, 64) == 0 and count(0, 1, 64) == 0
+
+
 @pytest.mark.parametrize("field,value", [("engine", 4), ("engine", -1), ("parts", 9), ("parts", -1),
                                          ("raster", -1), ("split_exact", 3), ("pace", -2),
                                          ("pace", 65537)])

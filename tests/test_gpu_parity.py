@@ -229,8 +229,28 @@ def test_diagonal_gemm_exact(api, orc, engine, s, D, k, m, n, monkeypatch):
     assert api.device_status() == 0
 
 
+@pytest.mark.parametrize("engine", ["0", "1"])
+@pytest.mark.parametrize("m,n", [(128, 256), (256, 512)])
+def test_diagonal_gemm_full_chunk_at_the_int32_bound(api, engine, m, n, monkeypatch):
+    """One digit pair (s = D = 1) with every product -2^14 over two whole
+    int32 chunks and a partial third: each whole chunk sums to -2032 * 64 *
+    2^14 = -2130706432, the largest magnitude the chunk length allows; the
+    diagonal must come back as -2^14 k exactly.  Both engines; m = 128 runs
+    the single-CTA tcgen05 kernel, m = 256 the CTA-pair kernel."""
+    monkeypatch.setenv("MDG_SLICE_ENGINE", engine)
+    k = 2 * 2032 * 64 + 640
+    assert api.lib().mdg_slice_chunk_count(1, 1, k) == 3
+    dA = torch.full((1, m, k), 128.0, dtype=torch.bfloat16, device="cuda")
+    dB = torch.full((1, n, k), -128.0, dtype=torch.bfloat16, device="cuda")
+    Cd = api.slice_diagonals(dA, dB, 1)
+    assert int(Cd[0].min()) == int(Cd[0].max()) == -2032 * 64 * 2 ** 14
+    diag = api.chunks_to_diagonals(Cd, 1, 1, k)
+    assert np.all(diag == -(2 ** 14) * k)
+    assert api.device_status() == 0
+
+
 @pytest.mark.parametrize("P,D", [(2, 14), (4, 28), (8, 55), (16, 110)])
-@pytest.mark.parametrize("k", [64, 64 * 2048])
+@pytest.mark.parametrize("k", [64, 64 * 4096])
 def test_renorm_bit_exact(api, orc, P, D, k):
     rng = np.random.default_rng(P + k)
     m, n, s = 9, 21, D
@@ -303,9 +323,9 @@ def test_slice_gemm_schedules_bit_identical(api, inputs, monkeypatch):
     """Tile order (raster), diagonal ranges per tile (parts) and the pacing
     of the CTA-pair kernel only reorder exact integer work: every schedule,
     and the mma.sync engine, must return the same bits.  36 pair tiles with
-    2560-deep k (diagonals span two int32 chunks); pace 1 makes the
-    producers hold at almost every check."""
-    P, m, n, k = 4, 1536, 1536, 2560
+    5120-deep k (the three longest diagonals span two int32 chunks); pace 1
+    makes the producers hold at almost every check."""
+    P, m, n, k = 4, 1536, 1536, 5120
     rng = np.random.default_rng(1536)
     A = dev(inputs.normal_pd(rng, (m, k), P))
     B = dev(inputs.normal_pd(rng, (k, n), P))
