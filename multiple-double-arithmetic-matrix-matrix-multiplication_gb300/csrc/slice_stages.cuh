@@ -284,7 +284,10 @@ __device__ __forceinline__ void emit_limbs(const uint64_t (&w)[NW], int scale, d
   }
 }
 
-template <int P, int NW, int V>
+// PAIRED: the first two chunk planes of each diagonal are loaded together
+// (the second load repeats the first when the diagonal has one chunk), so
+// that two loads are in flight where diagonals span two chunks.
+template <int P, int NW, int V, bool PAIRED = false>
 __device__ __forceinline__ void renorm_elems(int s, int D, int KB, int m, int n,
                                              const int *__restrict__ chunks, long long plane_c,
                                              int ldcd, const int *__restrict__ E,
@@ -311,7 +314,16 @@ __device__ __forceinline__ void renorm_elems(int s, int D, int KB, int m, int n,
         const int d = D - 1 - k;
         const int nc = mdgi::diag_chunks(d, s, KB);
         q -= nc;
-        for (int j = 0; j < nc; ++j) {
+        int j = 0;
+        if constexpr (PAIRED) {
+          int x[V], y[V];
+          IntV<V>::load(src + (size_t)q * plane_c, x);
+          IntV<V>::load(src + (size_t)(q + (nc > 1 ? 1 : 0)) * plane_c, y);
+#pragma unroll
+          for (int v = 0; v < V; ++v) T[v] += (long long)x[v] + (nc > 1 ? y[v] : 0);
+          j = 2;
+        }
+        for (; j < nc; ++j) {
           int x[V];
           IntV<V>::load(src + (size_t)(q + j) * plane_c, x);
 #pragma unroll
