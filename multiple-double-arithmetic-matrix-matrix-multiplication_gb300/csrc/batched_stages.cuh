@@ -31,35 +31,26 @@ __global__ void __launch_bounds__(256)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = 8 * lu + warp;
     if (r >= b.m) return;
-    double mx = 0.0;
-    for (int c = lane; c < b.k; c += 32) {
-      const double *x = b.A + ((size_t)r * b.lda + c) * P;
-      double v = fabs(x[0]);
-      for (int l = 1; l < P; ++l) v = v + fabs(x[l]);
-      mx = fmax(mx, v);
-    }
+    unsigned long long mx = 0;
+    for (int c = lane; c < b.k; c += 32)
+      mx = umax64(mx, abs_sum_bits(b.A + ((size_t)r * b.lda + c) * P, P));
 #pragma unroll
-    for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if (lane == 0) exps[b.offE + r] = scale_exp(mx);
+    for (int o = 16; o; o >>= 1) mx = umax64(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) exps[b.offE + r] = scale_exp(__longlong_as_double((long long)mx));
   } else {
-    __shared__ double red[8][32];
+    __shared__ unsigned long long red[8][32];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int c = 32 * (lu - b.scale_b_off) + tx;
-    double mx = 0.0;
-    if (c < b.n) {
-      for (int r = ty; r < b.k; r += 8) {
-        const double *x = b.B + ((size_t)r * b.ldb + c) * P;
-        double v = fabs(x[0]);
-        for (int l = 1; l < P; ++l) v = v + fabs(x[l]);
-        mx = fmax(mx, v);
-      }
-    }
+    unsigned long long mx = 0;
+    if (c < b.n)
+      for (int r = ty; r < b.k; r += 8)
+        mx = umax64(mx, abs_sum_bits(b.B + ((size_t)r * b.ldb + c) * P, P));
     red[ty][tx] = mx;
     __syncthreads();
     if (ty == 0 && c < b.n) {
 #pragma unroll
-      for (int y = 1; y < 8; ++y) mx = fmax(mx, red[y][tx]);
-      exps[b.offF + c] = scale_exp(mx);
+      for (int y = 1; y < 8; ++y) mx = umax64(mx, red[y][tx]);
+      exps[b.offF + c] = scale_exp(__longlong_as_double((long long)mx));
     }
   }
 }

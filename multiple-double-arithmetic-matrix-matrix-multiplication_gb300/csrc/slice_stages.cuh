@@ -12,34 +12,43 @@
 namespace mdgi {
 
 // ------------------------------------------------------------ exponents --
+// sum_l |x_l| of one entry (FP64 additions in limb order), as its bit
+// pattern: maxima of non-negative doubles are taken as 64-bit unsigned
+// integers, which orders them like the doubles and keeps the reductions off
+// the FP64 pipe (narrow on this GPU).  A NaN sum counts as 0, so that a
+// maximum skips it as a floating-point comparison would.
+__device__ __forceinline__ unsigned long long abs_sum_bits(const double *x, int P) {
+  double v = fabs(x[0]);
+  for (int l = 1; l < P; ++l) v = v + fabs(x[l]);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return b > 0x7ff0000000000000ull ? 0ull : b;
+}
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
+  return a > b ? a : b;
+}
+
 // Block 32 x 8 covers 32 columns x 256 rows; each warp walks 32 rows of
 // one 32-column strip.  Row maxima: warp reduction, one atomic per row per
-// warp.  Column maxima: one atomic per thread.  Maxima of non-negative
-// doubles are compared as 64-bit integers.
+// warp.  Column maxima: one atomic per thread.
 __device__ __forceinline__ void absmax_block(int P, int R, int Cn, const double *__restrict__ X,
                                              int ldx, unsigned long long *rowbits,
                                              unsigned long long *colbits, int bx, int by) {
   const int c = bx * 32 + threadIdx.x;
   const int r0 = by * 256 + threadIdx.y * 32;
-  double cm = 0.0;
+  unsigned long long cm = 0;
   for (int rr = 0; rr < 32; ++rr) {
     const int r = r0 + rr;
     if (r >= R) break;
-    double v = 0.0;
-    if (c < Cn) {
-      const double *x = X + ((size_t)r * ldx + c) * P;
-      v = fabs(x[0]);
-      for (int l = 1; l < P; ++l) v = v + fabs(x[l]);
-    }
-    cm = fmax(cm, v);
+    const unsigned long long v = c < Cn ? abs_sum_bits(X + ((size_t)r * ldx + c) * P, P) : 0ull;
+    cm = umax64(cm, v);
     if (rowbits) {
-      double w = v;
+      unsigned long long w = v;
 #pragma unroll
-      for (int o = 16; o; o >>= 1) w = fmax(w, __shfl_xor_sync(0xffffffffu, w, o));
-      if (threadIdx.x == 0) atomicMax(rowbits + r, (unsigned long long)__double_as_longlong(w));
+      for (int o = 16; o; o >>= 1) w = umax64(w, __shfl_xor_sync(0xffffffffu, w, o));
+      if (threadIdx.x == 0) atomicMax(rowbits + r, w);
     }
   }
-  if (colbits && c < Cn) atomicMax(colbits + c, (unsigned long long)__double_as_longlong(cm));
+  if (colbits && c < Cn) atomicMax(colbits + c, cm);
 }
 
 // --------------------------------------------------------------- digits --
