@@ -175,9 +175,11 @@ int plan_batch(const mdg_problem *problems, int count, Layout *L, mdg_batch_s *h
     const int nw = std::max(mdgi::words_for(s, 1), mdgi::words_for(1, D));
     if (!nw || nw > mdgi::batch_words(q.p)) return MDG_ERROR_NOT_SUPPORTED;
     h->nwmax = std::max(h->nwmax, mdgi::batch_words(q.p));
-    const int kblocks = (Kp + 127) / 128;
+    const int kblocks = (q.k + 127) / 128;
     const int scale_a = (q.m + 7) / 8, scale_b = (q.n + 31) / 32;
-    const int digit_a = Mp * kblocks, digit_b = Np * kblocks;
+    // digits: valid rows and k-positions only (the padding is cleared once,
+    // by mdg_batch_create)
+    const int digit_a = q.m * kblocks, digit_b = q.n * kblocks;
     const int out_u = q.m;  // renormalisation: one row of blocks per output row
     if (ws) {
       BatchProblem b{};
@@ -300,6 +302,18 @@ int mdg_batch_create(const mdg_problem *problems, int count, void *workspace,
   h->dgroups = reinterpret_cast<mdgi::GroupedProblem *>(ws + L.off_groups);
   h->exps = reinterpret_cast<int *>(ws + L.off_exps);
   cudaStream_t s = mdgi::as_stream(stream);
+  // zero digit planes: the digit kernel writes only the valid rows and
+  // k-positions of each problem, so the padding stays zero for every run
+  for (const BatchProblem &b : h->hprobs) {
+    cudaError_t e = cudaMemsetAsync(b.dA, 0, sizeof(__nv_bfloat16) * (size_t)b.s * b.Mp * b.Kp, s);
+    if (e == cudaSuccess)
+      e = cudaMemsetAsync(b.dB, 0, sizeof(__nv_bfloat16) * (size_t)b.s * b.Np * b.Kp, s);
+    if (e != cudaSuccess) {
+      mdgi::set_cuda_error(e);
+      delete h;
+      return MDG_ERROR_CUDA;
+    }
+  }
   // a tile policy and split mode tuned earlier for the same shapes, else
   // 256-column tiles, split
   int policy = MDG_BATCH_TILES_256, split = 1;

@@ -59,12 +59,15 @@ __global__ void __launch_bounds__(256)
 // of B's) over 128 k-positions, one per thread (one element per thread
 // keeps the wide integers of the octo- and hexa-double branches few, so
 // the merged kernel's register count stays near the single-width ones').
+// Only the valid rows and k-positions: the padding of every plane was
+// cleared when the plan was made and nothing writes it afterwards.
 template <int NW>
 __device__ __forceinline__ void digits_unit(const BatchProblem &b, const int *exps, int lu) {
-  const int kblocks = (b.Kp + 127) / 128;
+  const int kblocks = (b.k + 127) / 128;
   const bool side_b = lu >= b.dig_b_off;
   if (side_b) lu -= b.dig_b_off;
   const int prow = lu / kblocks, pc = (lu - prow * kblocks) * 128 + (int)threadIdx.x;
+  if (pc >= b.k) return;
   if (!side_b)
     digits_elem<NW>(b.p, b.s, b.m, b.k, b.A, b.lda, exps + b.offE, 0, b.dA, b.Kp, b.plane_a,
                     b.Mp, b.Kp, prow, pc);
