@@ -51,14 +51,16 @@ bool alloc_over_limit(size_t bytes) {
 // workspace argument (mdg_gemm_host, mdg_scale_exponents).  One per slot.
 // The buffers, streams and events belong to one device; a call on another
 // device releases them first.
-constexpr int kMaxPanels = 4;
+constexpr int kMaxPanels = 4, kMaxStrips = 2;
 struct DeviceCache {
   std::mutex mu;
   int dev = -1;
-  void *ptr[4] = {nullptr, nullptr, nullptr, nullptr};
-  size_t cap[4] = {0, 0, 0, 0};
+  // A, B, C, then one workspace per column strip of the host entry
+  void *ptr[3 + kMaxStrips] = {};
+  size_t cap[3 + kMaxStrips] = {};
   cudaStream_t streams[3] = {nullptr, nullptr, nullptr};  // compute, copies in, copies out
-  cudaEvent_t events[2 + 2 * kMaxPanels] = {};  // start, B in, A panels in, C panels done
+  // start, B strips in, A panels in, C blocks done
+  cudaEvent_t events[1 + kMaxStrips + kMaxPanels + kMaxPanels * kMaxStrips] = {};
   // caller holds mu
   int bind_device() {
     int d = 0;
@@ -77,7 +79,7 @@ struct DeviceCache {
     return MDG_SUCCESS;
   }
   void release_locked() {
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < 3 + kMaxStrips; ++i) {
       if (ptr[i]) cudaFree(ptr[i]);
       ptr[i] = nullptr;
       cap[i] = 0;
@@ -231,13 +233,17 @@ static size_t workspace_bytes(int form, int p, int m, int n, int k, const Opts &
 
 using namespace mdgi;
 
-// mdg_gemm_host for the BF16 form on tall problems: B is copied in and its
-// exponents and digits computed once, then A is copied in row panels on one
-// copy stream while the previous panel computes, and each finished panel of
-// C goes back on a second copy stream, so most of the host-link traffic hides
-// behind the tensor-core work.  Bits as one mdg_gemm (slice_panel).  The
-// work starts after everything queued before it on the legacy default
-// stream and the blocking streams, as the single-stream path would.
+// mdg_gemm_host for the BF16 form on tall problems: C is computed in blocks
+// of row panels of A (up to four) by column strips of B (two when n >=
+// 4096).  The first block waits only for the first strip of B and the
+// first panel of A; the other strips and panels are copied in on one copy
+// stream while earlier blocks compute (each strip's exponents and digits
+// are computed once, each panel's once), and every finished block of C goes
+// back on a second copy stream, so most of the host-link traffic hides
+// behind the tensor-core work.  Bits as one mdg_gemm (slice_panel_a,
+// slice_block).  The work starts after everything queued before it on the
+// legacy default stream and the blocking streams, as the single-stream
+// path would.
 static int host_slice_panels_issue(int p, const Opts &o, int m, int n, int k, const double *A,
                                    const double *B, double *C, double *dA, double *dB,
                                    double *dC);
@@ -256,30 +262,46 @@ static int host_slice_panels(int p, const Opts &o, int m, int n, int k, const do
 static int host_slice_panels_issue(int p, const Opts &o, int m, int n, int k, const double *A,
                                    const double *B, double *C, double *dA, double *dB,
                                    double *dC) {
-  NvtxRange range("mdg host: B, then A panels overlapped");
+  NvtxRange range("mdg host: B strips and A panels overlapped");
   const int want = std::min(kMaxPanels, m / 1024);
   const int mp = (int)align_up((m + want - 1) / want, 256);
   const int panels = (m + mp - 1) / mp;
-  const SlicePlan pl = make_slice_plan(p, o.slices, o.diagonals, mp, n, k);
-  if (pl.Mp > 65535 || pl.Np > 65535) return MDG_ERROR_NOT_SUPPORTED;
-  void *ws = nullptr;
-  MDG_TRY(g_cache.get(3, pl.total, &ws));
+  // strips of ns columns (a multiple of 256); with two strips and n >= 4096
+  // the last one holds at least n / 2 - 255 columns
+  const int strips = n >= 4096 ? kMaxStrips : 1;
+  const int ns = strips > 1 ? (int)align_up((n + strips - 1) / strips, 256) : n;
+  SlicePlan pls[kMaxStrips];
+  void *ws[kMaxStrips] = {};
+  for (int j = 0; j < strips; ++j) {
+    pls[j] = make_slice_plan(p, o.slices, o.diagonals, mp, std::min(ns, n - j * ns), k);
+    if (pls[j].Mp > 65535 || pls[j].Np > 65535) return MDG_ERROR_NOT_SUPPORTED;
+    MDG_TRY(g_cache.get(3 + j, pls[j].total, &ws[j]));
+  }
   MDG_TRY(g_cache.make_streams());
   cudaStream_t sc = g_cache.streams[0], si = g_cache.streams[1], so = g_cache.streams[2];
-  cudaEvent_t ev0 = g_cache.events[0], evB = g_cache.events[1];
-  cudaEvent_t *evA = g_cache.events + 2, *evC = g_cache.events + 2 + kMaxPanels;
-  const size_t row_a = sizeof(double) * (size_t)k * p, row_c = sizeof(double) * (size_t)n * p;
-  const size_t ea = (size_t)k * p, ec = (size_t)n * p;  // doubles per row
+  cudaEvent_t ev0 = g_cache.events[0];
+  cudaEvent_t *evB = g_cache.events + 1, *evA = evB + kMaxStrips, *evC = evA + kMaxPanels;
+  const size_t ea = (size_t)k * p, ec = (size_t)n * p;  // doubles per row of A / of B and C
+  const size_t row_a = sizeof(double) * ea, pitch = sizeof(double) * ec;
   MDG_TRY_CUDA(cudaEventRecord(ev0, 0));
   MDG_TRY_CUDA(cudaStreamWaitEvent(si, ev0, 0));
   MDG_TRY_CUDA(cudaStreamWaitEvent(sc, ev0, 0));
-  MDG_TRY_CUDA(cudaMemcpyAsync(dB, B, sizeof(double) * (size_t)k * n * p, cudaMemcpyHostToDevice,
-                               si));
-  MDG_TRY_CUDA(cudaEventRecord(evB, si));
+  // copies in, in the order the blocks need them: strip 0 of B, panel 0 of
+  // A, the other strips, then (in the loop) the next panel of A
+  auto copy_strip = [&](int j) -> int {
+    const size_t c0 = (size_t)j * ns * p;
+    MDG_TRY_CUDA(cudaMemcpy2DAsync(dB + c0, pitch, B + c0, pitch,
+                                   sizeof(double) * (size_t)pls[j].n * p, k,
+                                   cudaMemcpyHostToDevice, si));
+    MDG_TRY_CUDA(cudaEventRecord(evB[j], si));
+    return MDG_SUCCESS;
+  };
+  MDG_TRY(copy_strip(0));
   MDG_TRY_CUDA(cudaMemcpyAsync(dA, A, row_a * std::min(mp, m), cudaMemcpyHostToDevice, si));
   MDG_TRY_CUDA(cudaEventRecord(evA[0], si));
-  MDG_TRY_CUDA(cudaStreamWaitEvent(sc, evB, 0));
-  MDG_TRY(slice_prepare_b(pl, dB, n, ws, sc));
+  for (int j = 1; j < strips; ++j) MDG_TRY(copy_strip(j));
+  MDG_TRY_CUDA(cudaStreamWaitEvent(sc, evB[0], 0));
+  MDG_TRY(slice_prepare_b(pls[0], dB, n, ws[0], sc));
   const int engine = engine_choice(o.engine);
   for (int i = 0; i < panels; ++i) {
     const int r0 = i * mp, rows = std::min(mp, m - r0);
@@ -290,12 +312,23 @@ static int host_slice_panels_issue(int p, const Opts &o, int m, int n, int k, co
       MDG_TRY_CUDA(cudaEventRecord(evA[i + 1], si));
     }
     MDG_TRY_CUDA(cudaStreamWaitEvent(sc, evA[i], 0));
-    MDG_TRY(slice_panel(pl, rows, dA + r0 * ea, k, dC + r0 * ec, n, ws, engine, o.parts, o.raster,
-                        sc, o.pace));
-    MDG_TRY_CUDA(cudaEventRecord(evC[i], sc));
-    MDG_TRY_CUDA(cudaStreamWaitEvent(so, evC[i], 0));
-    MDG_TRY_CUDA(cudaMemcpyAsync(C + r0 * ec, dC + r0 * ec, row_c * rows, cudaMemcpyDeviceToHost,
-                                 so));
+    // the panel's exponents and digits live in strip 0's workspace
+    MDG_TRY(slice_panel_a(pls[0], rows, dA + r0 * ea, k, ws[0], sc));
+    for (int j = 0; j < strips; ++j) {
+      if (i == 0 && j > 0) {
+        MDG_TRY_CUDA(cudaStreamWaitEvent(sc, evB[j], 0));
+        MDG_TRY(slice_prepare_b(pls[j], dB + (size_t)j * ns * p, n, ws[j], sc));
+      }
+      const size_t off = r0 * ec + (size_t)j * ns * p;
+      MDG_TRY(slice_block(pls[0], ws[0], pls[j], ws[j], rows, dC + off, n, engine, o.parts,
+                          o.raster, sc, o.pace));
+      cudaEvent_t done = evC[i * kMaxStrips + j];
+      MDG_TRY_CUDA(cudaEventRecord(done, sc));
+      MDG_TRY_CUDA(cudaStreamWaitEvent(so, done, 0));
+      MDG_TRY_CUDA(cudaMemcpy2DAsync(C + off, pitch, dC + off, pitch,
+                                     sizeof(double) * (size_t)pls[j].n * p, rows,
+                                     cudaMemcpyDeviceToHost, so));
+    }
   }
   MDG_TRY_CUDA(cudaStreamSynchronize(si));
   MDG_TRY_CUDA(cudaStreamSynchronize(sc));

@@ -354,8 +354,8 @@ int slice_prepare_b(const SlicePlan &pl, const double *B, int ldb, void *ws, cud
                        pl.plane_b, pl.Np, pl.Kp, st);
 }
 
-int slice_panel(const SlicePlan &pl, int rows, const double *A, int lda, double *C, int ldc,
-                void *ws, int engine, int parts, int raster, cudaStream_t st, int pace) {
+int slice_panel_a(const SlicePlan &pl, int rows, const double *A, int lda, void *ws,
+                  cudaStream_t st) {
   if (rows <= 0) return MDG_SUCCESS;
   if (rows > pl.m) return MDG_ERROR_INVALID_SIZE;
   char *base = reinterpret_cast<char *>(ws);
@@ -363,25 +363,45 @@ int slice_panel(const SlicePlan &pl, int rows, const double *A, int lda, double 
   auto *colbits = reinterpret_cast<unsigned long long *>(base + pl.off_colbits);
   int *E = reinterpret_cast<int *>(base + pl.off_E);
   int *F = reinterpret_cast<int *>(base + pl.off_F);
-  void *dA = base + pl.off_dA;
-  void *dB = base + pl.off_dB;
-  auto *Cd = reinterpret_cast<int *>(base + pl.off_Cd);
   // E only (n = 0 leaves F, computed by slice_prepare_b, alone)
   MDG_TRY(launch_scale_exponents(pl.p, rows, 0, pl.k, A, lda, nullptr, 1, rowbits, colbits, E,
                                  F, st));
   // rows beyond `rows` up to the plan's padded Mp get zero digits
-  MDG_TRY(launch_digits(pl.p, pl.s, rows, pl.k, A, lda, E, 0, dA, pl.Kp, pl.plane_a, pl.Mp,
-                        pl.Kp, st));
+  return launch_digits(pl.p, pl.s, rows, pl.k, A, lda, E, 0, base + pl.off_dA, pl.Kp,
+                       pl.plane_a, pl.Mp, pl.Kp, st);
+}
+
+int slice_block(const SlicePlan &pla, const void *wsa, const SlicePlan &plb, void *wsb, int rows,
+                double *C, int ldc, int engine, int parts, int raster, cudaStream_t st,
+                int pace) {
+  if (rows <= 0) return MDG_SUCCESS;
+  if (rows > pla.m || pla.Mp != plb.Mp || pla.Kp != plb.Kp || pla.s != plb.s ||
+      pla.D != plb.D || pla.p != plb.p)
+    return MDG_ERROR_INVALID_SIZE;
+  const char *abase = reinterpret_cast<const char *>(wsa);
+  char *bbase = reinterpret_cast<char *>(wsb);
+  const int *E = reinterpret_cast<const int *>(abase + pla.off_E);
+  const int *F = reinterpret_cast<const int *>(bbase + plb.off_F);
+  const void *dA = abase + pla.off_dA;
+  const void *dB = bbase + plb.off_dB;
+  auto *Cd = reinterpret_cast<int *>(bbase + plb.off_Cd);
+  const SlicePlan &pl = plb;
   if (engine != 0) {
-    MDG_TRY(launch_diag_gemm_tc(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
+    MDG_TRY(launch_diag_gemm_tc(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pla.plane_a,
                                 pl.plane_b, Cd, pl.plane_c, engine == 2 ? 1 : 0, parts, raster, st,
                                 pace));
   } else {
-    MDG_TRY(launch_diag_gemm_v0(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pl.plane_a,
+    MDG_TRY(launch_diag_gemm_v0(pl.s, pl.D, pl.Mp, pl.Np, pl.Kp, dA, dB, pl.Kp, pla.plane_a,
                                 pl.plane_b, Cd, pl.plane_c, st));
   }
   return launch_renorm(pl.p, pl.s, pl.D, pl.Kp / 64, rows, pl.n, Cd, pl.plane_c, pl.Np, E, F, C,
                        ldc, st);
+}
+
+int slice_panel(const SlicePlan &pl, int rows, const double *A, int lda, double *C, int ldc,
+                void *ws, int engine, int parts, int raster, cudaStream_t st, int pace) {
+  MDG_TRY(slice_panel_a(pl, rows, A, lda, ws, st));
+  return slice_block(pl, ws, pl, ws, rows, C, ldc, engine, parts, raster, st, pace);
 }
 
 int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *B, int ldb,

@@ -134,6 +134,18 @@ int run_slice_gemm(const SlicePlan &pl, const double *A, int lda, const double *
 int slice_prepare_b(const SlicePlan &pl, const double *B, int ldb, void *ws, cudaStream_t st);
 int slice_panel(const SlicePlan &pl, int rows, const double *A, int lda, double *C, int ldc,
                 void *ws, int engine, int parts, int raster, cudaStream_t st, int pace = 0);
+// slice_panel in two parts, for callers that also split B into column
+// strips (each with its own plan and workspace, prepared by
+// slice_prepare_b): slice_panel_a computes the exponents and digits of
+// rows (<= pla.m) rows of A into wsa; slice_block then computes those rows
+// of C against the strip of plb / wsb (plans of equal m, k, s, D).  Every
+// column of C depends only on its column of B, so blocks give the bits of
+// one run_slice_gemm.
+int slice_panel_a(const SlicePlan &pl, int rows, const double *A, int lda, void *ws,
+                  cudaStream_t st);
+int slice_block(const SlicePlan &pla, const void *wsa, const SlicePlan &plb, void *wsb, int rows,
+                double *C, int ldc, int engine, int parts, int raster, cudaStream_t st,
+                int pace = 0);
 
 // Which engine mdg_gemm uses for the BF16 form (MDG_SLICE_ENGINE=0/1 overrides).
 int default_engine();

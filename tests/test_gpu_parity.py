@@ -478,12 +478,13 @@ def test_host_entry_with_library_pinned_buffers(api, inputs):
     assert L.mdg_host_alloc(8, None) == 3
 
 
-@pytest.mark.parametrize("m,n,k", [(2600, 300, 200), (4500, 130, 70)])
+@pytest.mark.parametrize("m,n,k", [(2600, 300, 200), (4500, 130, 70), (2600, 4300, 96)])
 def test_pipelined_host_entry_matches_device_entry(api, inputs, m, n, k):
     """mdg_gemm_host of the BF16 form on m >= 2048 rows copies A in row
     panels overlapped with the computation (2 panels of 1536 + 1064 rows,
-    4 panels of 3 x 1280 + 660): the bits equal one device-side mdg_gemm.
-    Run twice so the second call reuses the library's buffers and streams."""
+    4 panels of 3 x 1280 + 660) and, for n >= 4096, B in two column strips
+    (2304 + 1996 columns): the bits equal one device-side mdg_gemm.  Run
+    twice so the second call reuses the library's buffers and streams."""
     P, A, B = inputs.workload("qd1024", m, n, k)
     dC = host(api.gemm(dev(A), dev(B), "slice_bf16"))
     for _ in range(2):
