@@ -775,9 +775,9 @@ def main():
             "e2e": {"value": flops * world / t_e2e / 1e9, "unit": UNIT,
                     "h2d_bytes_per_step": A.nbytes + B.nbytes,
                     "d2h_bytes_per_step": m * n * P * 8,
-                    "call": "mdg_gemm_host (page-locked host buffers from mdg_host_alloc; B, "
-                            "then A in row panels overlapped with the GEMM, C panels copied "
-                            "back behind it)",
+                    "call": "mdg_gemm_host (page-locked host buffers from mdg_host_alloc; "
+                            "blocks of A row panels by B column strips, copies in overlapped "
+                            "with the GEMM, C blocks copied back behind it)",
                     "steps": e2e_steps,
                     "h2d_gbs": A.nbytes / t_h2d / 1e9,
                     "h2d_gbs_first_copy": A.nbytes / t_h2d_first / 1e9,
