@@ -324,9 +324,10 @@ def pipelined_e2e(api, hA, hB, hC, P, m, n, k, ws_bytes, steps):
 def batched_tile_work(probs, slices, policy="256"):
     """BF16 FLOP of the batched diagonal GEMM at the given digit counts per
     P: useful (2 m n k per digit pair of the s diagonals kept) and as the
-    grouped kernel pads it (rows to 128, columns to the tile width of the
-    policy, k to 16: the last 64-deep block issues only the MMAs that reach
-    data)."""
+    grouped kernel pads it: single-CTA tiles pad rows to 128, columns to the
+    tile width of the policy and k to 16 (the last 64-deep block issues only
+    the MMAs that reach data); CTA-pair tiles pad rows and columns to 256
+    and k to 64."""
     def pairs(s):
         return sum(min(d, s - 1) - max(0, d - (s - 1)) + 1 for d in range(s))
     up = lambda x, a: -(-x // a) * a
@@ -340,7 +341,10 @@ def batched_tile_work(probs, slices, policy="256"):
     for P, m, n, k in probs:
         q = pairs(slices[P])
         useful += 2.0 * m * n * k * q
-        padded += 2.0 * up(m, 128) * width(n) * up(k, 16) * q
+        if policy == "pair":
+            padded += 2.0 * up(m, 256) * up(n, 256) * up(k, 64) * q
+        else:
+            padded += 2.0 * up(m, 128) * width(n) * up(k, 16) * q
     return useful, padded
 
 
