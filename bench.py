@@ -56,7 +56,7 @@ WORKLOADS = {
 # the paced CTA-pair diagonal GEMM, from one-pass ncu captures of the bench's
 # own command on this machine's GB300 (quad-double, seed 4 inputs):
 #   8192^3: 462.35 GB read + 17.27 GB written;  4096^3: 71.66 + 2.69 GB.
-DIAG_TRAFFIC_BYTES = {"qd8192_normal": 479.62e9, "qd4096_normal": 74.35e9}
+DIAG_TRAFFIC_BYTES = {"qd8192_normal": 473.09e9, "qd4096_normal": 73.51e9}
 
 
 DEFAULT_SLICES = {2: 14, 4: 28, 8: 55, 16: 110}
