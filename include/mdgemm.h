@@ -30,7 +30,7 @@ typedef enum {
   MDG_ERROR_INVALID_FORM = 4,   /* unknown form or option value */
   MDG_ERROR_WORKSPACE = 5,      /* workspace missing or smaller than *_workspace_size */
   MDG_ERROR_CUDA = 6,           /* a CUDA call failed, see mdg_last_cuda_error() */
-  MDG_ERROR_NOT_SUPPORTED = 7,  /* valid request this build cannot serve */
+  MDG_ERROR_NOT_SUPPORTED = 7,  /* valid request the library cannot serve */
   MDG_ERROR_TIMEOUT = 8,        /* a bounded device-side wait gave up */
   MDG_ERROR_ALLOCATION = 9,     /* device or pinned allocation failed */
   MDG_ERROR_TOO_LARGE = 10      /* problem needs more than the fixed scratch of mdg_gemm_slice_static */
