@@ -12,8 +12,8 @@ tolerance of the small-size test.
 
 Workloads (quad-double 1024^3 seed 1, octo-double 2048^3 seed 2 with row
 and column scales 2^U{-32..32}, quad-double 8192^3 seed 4 with N(0, 1) hi
-limbs, double-double 64^3 seed 0): synthetic seeded inputs with the
-benchmark's shapes and distributions.
+limbs, double-double 64^3 seed 0, and the 256 mixed problems of seed 3):
+synthetic seeded inputs with the benchmark's shapes and distributions.
 """
 import numpy as np
 import pytest
@@ -114,3 +114,31 @@ def test_fp64split_form_full_size_block_error_bits(api, orc, inputs, name):
     bits_ref = ex.error_bits(want, Ab, Bb, r, c)
     print(name, "fp64split", bits, "oracle", bits_ref)
     assert bits[1] >= bits_ref[1] - 2.0, (bits, bits_ref)
+
+
+def test_batched_workload_equals_single_problem_gemms(api, orc, inputs):
+    """The whole 256-problem batched workload (seed 3) as one plan, tuned
+    (tile policy and split mode) and replayed: every problem's C equals its
+    single-problem BF16 GEMM bit for bit, and a sampled block of one
+    octo-double problem equals the oracle."""
+    probs, rng = inputs.batched_problems(256, seed=3)
+    ops = [(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda())
+           for A, B in inputs.batched_operands(probs, rng)]
+    plan = api.BatchPlan(ops)
+    api.tune_cache_clear()
+    plan.tune()
+    api.tune_cache_clear()
+    for C in plan.Cs:
+        C.fill_(float("nan"))
+    plan.run()
+    torch.cuda.synchronize()
+    assert api.device_status() == 0
+    for i, ((A, B), C) in enumerate(zip(ops, plan.Cs)):
+        assert torch.equal(C, api.gemm(A, B, "slice_bf16")), (i, probs[i])
+    i = next(j for j, pr in enumerate(probs) if pr[0] == 8)
+    P, m, n, k = probs[i]
+    rows, cols = sample(6, m, 47), sample(6, n, 53)
+    Ab, Bb = block_inputs(ops[i][0].cpu().numpy(), ops[i][1].cpu().numpy(), rows, cols)
+    s = api.default_slices(P)
+    got = plan.Cs[i].cpu().numpy()[np.ix_(rows, cols)]
+    assert np.array_equal(got, orc.gemm_slices(P, s, s, Ab, Bb, len(rows), len(cols), k))
